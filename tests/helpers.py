@@ -1,0 +1,36 @@
+"""Shared set-up of the parity tests: ccp parameter texts, engine <-> oracle
+glue and the force-error measures."""
+import math
+
+import numpy as np
+
+RCO = 1.154701
+
+
+def ccp_params(N, cvf=0.2, laf=0.25, extra=""):
+    """adjustable-parameters text as Scripts/makeallsim.py:44-87 derives it."""
+    R = RCO / 2 + RCO / 2 * (N / cvf) ** (1 / 3)
+    n_l = int(math.floor(laf * 4 / ((0.5 / (R - RCO)) ** 2)))
+    txt = "number_of_particles %05d\nnucleus_radius %09.6f\nnumber_of_lbs %05d\n" % (N, R, n_l)
+    return txt + extra, R, n_l
+
+
+def baseline_params(N, extra=""):
+    return "force_field baseline\nnumber_of_particles %d\n" % N + extra
+
+
+def heads_of(sim, s=0):
+    si = sim.system_info(s)
+    L = si.n_beads // si.n_chains
+    return [c * L for c in range(si.n_chains)]
+
+
+def force_errors(f_gpu, f_ref, absum):
+    """(max relative error |dF|/|F| over beads with |F| >= 1e-3 * S, and the
+    max of |dF| / S) where S is the sum of the magnitudes of the force terms."""
+    d = np.linalg.norm(np.asarray(f_gpu, np.float64) - f_ref, axis=1)
+    n = np.linalg.norm(f_ref, axis=1)
+    big = n >= 1e-3 * absum
+    rel = (d[big] / n[big]).max() if big.any() else 0.0
+    scaled = (d / np.maximum(absum, 1e-30)).max()
+    return rel, scaled

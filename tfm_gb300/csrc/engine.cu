@@ -1,0 +1,1085 @@
+// Batched GB300 Brownian-dynamics engine and its C ABI (include/ccpgpu.h).
+//
+// Memory layout in HBM (all systems concatenated, chain order):
+//   pos, er          float4 per bead: x, y, z, flags (BF_*) in w
+//   fbuf             float4 per bead: stage-1 force (f of chrsim.cu:387)
+//   sorted           float4 per bead in cell order: x, y, z, (index << 3 | flags)
+//   fs               float4 per bead in cell order: pair force
+//   rank             uint32 per bead: rank of the bead inside its cell
+//   counts, start    uint32 per cell (+1): histogram and exclusive prefix
+// Cells of system s occupy [cell_off, cell_off + cps^3); because every system
+// lives in its own cells, the counting sort keeps each system's beads inside
+// its own slot range [bead_off, bead_off + n).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ccpgpu.h"
+#include "host.h"
+#include "kernels.cuh"
+
+namespace ccpgpu {
+
+#define CK(x)                                                                      \
+  do {                                                                             \
+    cudaError_t e_ = (x);                                                          \
+    if (e_ != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  void alloc(size_t n_) {
+    release();
+    n = n_;
+    if (n) CK(cudaMalloc(&p, n * sizeof(T)));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+constexpr int TILE = 128;
+
+struct Engine {
+  Params par;
+  ForceField ff{};
+  std::vector<SystemSpec> specs;
+  std::vector<SysDesc> hsys;
+  std::vector<Geometry> geo;
+  std::vector<Tile> htiles;
+  int nb = 0, nc = 0, nl = 0, nch = 0;
+  int nblk = 0;        // scan CTAs
+  int64_t map_total = 0;
+  int ps_total = 0;
+
+  // host state
+  std::vector<float> hxyz;     // chain-order positions
+  std::vector<int32_t> hpt;    // ccp type codes
+  std::vector<float> hlbs;     // LBS positions, per system in placement order
+  std::vector<uint32_t> hflags;
+  std::vector<int32_t> chain_of, chain_first, chain_len, chain_ps_off, chain_smax, chain_sys;
+  std::vector<uint32_t> i_f;
+  std::vector<float> t;
+  uint64_t step = 0;
+  uint64_t dev_next = ~0ull;  // step the device counter will produce next
+  int frames_observed = 0;
+  bool positions_valid = false;
+
+  // device state
+  DevBuf<SysDesc> d_sys;
+  DevBuf<Tile> d_tiles;
+  DevBuf<float4> pos, er, fbuf, fs, sorted, lbs_sorted, fout;
+  DevBuf<uint32_t> rank, counts, start, bsum, lbs_start;
+  DevBuf<int32_t> d_chain_of, d_chain_first, d_chain_len, d_chain_ps_off, d_chain_smax;
+  DevBuf<int32_t> map, ps;
+  DevBuf<double> obs, ds;
+  DevBuf<unsigned long long> ovl, d_step;
+  DevBuf<int> d_err;
+  DevBuf<float> xyz_stage;
+  float *pinned[2] = {nullptr, nullptr};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+
+  ~Engine() {
+    for (auto &g : graphs) cudaGraphExecDestroy(g.second);
+    for (int k = 0; k < 2; ++k) {
+      if (pinned[k]) cudaFreeHost(pinned[k]);
+      if (ev[k]) cudaEventDestroy(ev[k]);
+    }
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  // -------------------------------------------------------------- setup
+  void build(const Params &p, std::vector<SystemSpec> sp) {
+    par = p;
+    ff = p.ff;
+    specs = std::move(sp);
+    int ns = (int)specs.size();
+    hsys.resize(ns);
+    geo.resize(ns);
+    i_f.assign(ns, 0);
+    t.assign(ns, 0.0f);
+    nb = nc = nl = nch = 0;
+    map_total = 0;
+    ps_total = 0;
+    chain_of.clear();
+    chain_first.clear();
+    chain_len.clear();
+    chain_ps_off.clear();
+    chain_smax.clear();
+    chain_sys.clear();
+    for (int s = 0; s < ns; ++s) {
+      SystemSpec &q = specs[s];
+      Geometry g = make_geometry(q.R_n, q.R_o, q.R_b);
+      geo[s] = g;
+      SysDesc d{};
+      d.bead_off = nb;
+      d.n = q.n;
+      d.csl = p.cell_side;
+      d.inv_csl = 1.0f / p.cell_side;
+      d.cps = 2 * (int)std::ceil(g.d_m / p.cell_side);
+      if (d.cps < 2) d.cps = 2;
+      d.cell_off = nc;
+      d.R_n = g.R_n;
+      d.R_o = g.R_o;
+      d.R_b = g.R_b;
+      d.noc = g.noc;
+      d.boc = g.boc;
+      d.nod = g.nod;
+      d.bod = g.bod;
+      d.lbs_off = nl;
+      d.n_lbs = q.n_lbs;
+      d.seed_lo = (uint32_t)q.seed;
+      d.seed_hi = (uint32_t)(q.seed >> 32);
+      d.chain_off = nch;
+      d.sys_index = s;
+      // chains
+      std::vector<int> heads = q.chain_first;
+      if (heads.empty()) {
+        int L = q.n / q.n_chains;
+        for (int c = 0; c < q.n_chains; ++c) heads.push_back(c * L);
+      }
+      d.n_chains = (int)heads.size();
+      for (int c = 0; c < d.n_chains; ++c) {
+        int b = heads[c], e = (c + 1 < d.n_chains) ? heads[c + 1] : q.n;
+        chain_first.push_back(nb + b);
+        chain_len.push_back(e - b);
+        chain_smax.push_back((e - b) / 2);
+        chain_ps_off.push_back(ps_total);
+        chain_sys.push_back(s);
+        ps_total += (e - b) / 2 + 1;
+        for (int i = b; i < e; ++i) chain_of.push_back(nch + c);
+      }
+      nch += d.n_chains;
+      // contact map binning (chrana.cu:187-189 for the ccp pixels)
+      bool diploid = (p.preset == PRESET_CCP && (uint32_t)q.n == CCP_N_DEF && d.n_chains == 12);
+      d.n_copies = diploid ? 2 : 1;
+      d.copy_len = q.n / d.n_copies;
+      if (q.contact_bins > 0) {
+        d.nbins = std::min(q.contact_bins, d.copy_len);
+        d.map_len = d.copy_len;
+      } else {
+        d.nbins = d.copy_len / CCP_PX_SZ;
+        d.map_len = d.nbins * CCP_PX_SZ;
+      }
+      if (d.nbins < 1) {
+        d.nbins = 1;
+        d.map_len = d.copy_len;
+      }
+      d.map_off = map_total;
+      map_total += (int64_t)d.nbins * (d.nbins + 1) / 2;
+      hsys[s] = d;
+      nb += q.n;
+      nc += d.cps * d.cps * d.cps;
+      nl += q.n_lbs;
+    }
+    htiles.clear();
+    for (int s = 0; s < ns; ++s)
+      for (int b = 0; b < hsys[s].n; b += TILE) htiles.push_back(Tile{s, hsys[s].bead_off + b});
+    nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
+
+    hxyz.assign((size_t)3 * nb, 0.0f);
+    hpt.assign(nb, 1);
+    hlbs.assign((size_t)3 * nl, 0.0f);
+    hflags.assign(nb, 0);
+
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+    d_sys.alloc(ns);
+    d_tiles.alloc(htiles.size());
+    pos.alloc(nb + 1);
+    er.alloc(nb + 1);
+    fbuf.alloc(nb + 1);
+    fs.alloc(nb + 1);
+    sorted.alloc(nb + 1);
+    fout.alloc(nb + 1);
+    rank.alloc(nb + 1);
+    size_t cpad = (size_t)nblk * SCAN_CHUNK;
+    counts.alloc(cpad);
+    start.alloc(cpad + 4);
+    bsum.alloc(nblk + 1);
+    lbs_sorted.alloc(std::max(nl, 1));
+    lbs_start.alloc(nc + 1);
+    d_chain_of.alloc(nb);
+    d_chain_first.alloc(nch);
+    d_chain_len.alloc(nch);
+    d_chain_ps_off.alloc(nch);
+    d_chain_smax.alloc(nch);
+    map.alloc(std::max<int64_t>(map_total, 1));
+    ps.alloc(std::max(ps_total, 1));
+    ds.alloc(std::max(ps_total, 1));
+    obs.alloc((size_t)ns * OBS_STRIDE);
+    ovl.alloc(ns);
+    d_step.alloc(1);
+    d_err.alloc(ERR_COUNT);
+    xyz_stage.alloc((size_t)3 * nb);
+    for (int k = 0; k < 2; ++k) CK(cudaMallocHost(&pinned[k], sizeof(float) * 3 * std::max(nb, 1)));
+
+    CK(cudaMemcpyAsync(d_sys.p, hsys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tiles.p, htiles.data(), sizeof(Tile) * htiles.size(),
+                       cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_chain_of.p, chain_of.data(), 4 * nb, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_chain_first.p, chain_first.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_chain_len.p, chain_len.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_chain_ps_off.p, chain_ps_off.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_chain_smax.p, chain_smax.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * cpad, stream));
+    CK(cudaMemsetAsync(start.p, 0, sizeof(uint32_t) * (cpad + 4), stream));
+    CK(cudaMemsetAsync(d_err.p, 0, sizeof(int) * ERR_COUNT, stream));
+    CK(cudaMemsetAsync(pos.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(er.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(fbuf.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(fs.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(sorted.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(lbs_start.p, 0, sizeof(uint32_t) * (nc + 1), stream));
+    reset_observables();
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  // -------------------------------------------------------------- uploads
+  void set_chain_flags() {
+    for (int i = 0; i < nb; ++i) hflags[i] = type_to_flags(hpt[i], par.preset);
+    for (int c = 0; c < nch; ++c) hflags[chain_first[c]] |= BF_START;
+  }
+
+  // Uploads positions + flags and rebuilds the cell histogram of pos.
+  void upload_positions() {
+    set_chain_flags();
+    std::vector<float4> v(nb + 1);
+    for (int i = 0; i < nb; ++i) {
+      uint32_t w = hflags[i];
+      float wf;
+      std::memcpy(&wf, &w, 4);
+      v[i] = make_float4(hxyz[3 * i], hxyz[3 * i + 1], hxyz[3 * i + 2], wf);
+    }
+    uint32_t ws = BF_START;
+    float wsf;
+    std::memcpy(&wsf, &ws, 4);
+    v[nb] = make_float4(0, 0, 0, wsf);
+    CK(cudaMemcpyAsync(pos.p, v.data(), sizeof(float4) * (nb + 1), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    recount();
+    positions_valid = true;
+  }
+
+  void recount() {
+    CK(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (size_t)nblk * SCAN_CHUNK, stream));
+    k_count<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, counts.p,
+                                                           rank.p, d_err.p);
+    CK(cudaGetLastError());
+  }
+
+  // LBS of every system sorted by cell (static during a run).
+  void upload_lbs() {
+    std::vector<uint32_t> cnt(nc + 1, 0);
+    std::vector<int> cell_of_l(nl);
+    for (size_t s = 0; s < hsys.size(); ++s) {
+      const SysDesc &d = hsys[s];
+      for (int k = 0; k < d.n_lbs; ++k) {
+        int l = d.lbs_off + k;
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+          float v = hlbs[3 * l + a];
+          float f = std::floor(v * d.inv_csl) + (float)(d.cps >> 1);
+          int ci = (f >= 0.0f) ? ((f >= (float)d.cps) ? d.cps - 1 : (int)f) : 0;
+          c[a] = ci;
+        }
+        int cl = d.cell_off + (c[2] * d.cps + c[1]) * d.cps + c[0];
+        cell_of_l[l] = cl;
+        cnt[cl]++;
+      }
+    }
+    std::vector<uint32_t> st(nc + 1, 0);
+    uint32_t acc = 0;
+    for (int c = 0; c < nc; ++c) {
+      st[c] = acc;
+      acc += cnt[c];
+    }
+    st[nc] = acc;
+    std::vector<float4> srt(std::max(nl, 1));
+    std::vector<uint32_t> fill(st.begin(), st.end());
+    for (int l = 0; l < nl; ++l) {
+      uint32_t slot = fill[cell_of_l[l]]++;
+      srt[slot] = make_float4(hlbs[3 * l], hlbs[3 * l + 1], hlbs[3 * l + 2], 0.0f);
+    }
+    CK(cudaMemcpyAsync(lbs_sorted.p, srt.data(), sizeof(float4) * std::max(nl, 1),
+                       cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(lbs_start.p, st.data(), sizeof(uint32_t) * (nc + 1), cudaMemcpyHostToDevice,
+                       stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  void download_positions() {
+    k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(pos.p, xyz_stage.p, nb);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hxyz.data(), xyz_stage.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost,
+                       stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  // -------------------------------------------------------------- launches
+  void launch_scan(bool bump) {
+    k_scan_reduce<<<nblk, SCAN_THREADS, 0, stream>>>(counts.p, bsum.p);
+    k_scan_top<<<1, SCAN_TOP_THREADS, 0, stream>>>(bsum.p, nblk, d_step.p, bump ? 1 : 0);
+    k_scan_apply<<<nblk, SCAN_THREADS, 0, stream>>>(counts.p, bsum.p, start.p, nc, nblk);
+  }
+
+  void launch_scatter(const float4 *src) {
+    k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, src, rank.p,
+                                                             start.p, sorted.p, d_err.p);
+  }
+
+  template <int MODE>
+  void launch_pair() {
+    k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                                start.p, fs.p);
+  }
+
+  template <int STAGE, int MODE>
+  void launch_update() {
+    k_update<STAGE, MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+        d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, start.p, counts.p,
+        lbs_sorted.p, lbs_start.p, d_step.p, d_err.p);
+  }
+
+  ContactArgs contact_args(bool do_map, bool do_ps, bool do_ovl) {
+    ContactArgs a;
+    a.cut = par.contact_cutoff;
+    a.mis = CCP_MIS;
+    a.do_map = do_map;
+    a.do_ps = do_ps;
+    a.do_overlap = do_ovl;
+    a.map = map.p;
+    a.ps = ps.p;
+    a.chain_of = d_chain_of.p;
+    a.chain_first = d_chain_first.p;
+    a.chain_ps_off = d_chain_ps_off.p;
+    a.chain_smax = d_chain_smax.p;
+    a.overlaps = ovl.p;
+    return a;
+  }
+
+  // Observables on the cell-ordered copy of pos (must be current).
+  void launch_observe_sorted(bool with_sdist) {
+    k_contacts<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p, start.p,
+                                                              contact_args(true, true, false));
+    k_observe<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p,
+                                                             CCP_RCO / 2.0f, obs.p);
+    if (with_sdist) {
+      int smax = 0, lmax = 0;
+      for (int c = 0; c < nch; ++c) {
+        smax = std::max(smax, chain_smax[c]);
+        lmax = std::max(lmax, chain_len[c]);
+      }
+      if (smax > 0) {
+        for (int c = 0; c < nch; ++c) {
+          dim3 grid((chain_smax[c] + 127) / 128, (chain_len[c] + SDIST_PCHUNK - 1) / SDIST_PCHUNK);
+          if (chain_smax[c] == 0) continue;
+          k_sdist<<<grid, 128, 0, stream>>>(pos.p, d_chain_first.p, d_chain_len.p,
+                                            d_chain_ps_off.p, d_chain_smax.p, c, ds.p);
+        }
+      }
+    }
+  }
+
+  template <int MODE>
+  void launch_step(bool observe) {
+    launch_scan(true);
+    launch_scatter(pos.p);
+    if (observe) launch_observe_sorted(false);
+    launch_pair<MODE>();
+    launch_update<1, MODE>();
+    launch_scan(false);
+    launch_scatter(er.p);
+    launch_pair<MODE>();
+    launch_update<2, MODE>();
+  }
+
+  // Graph of n steps; when obs is set the state at the first step is observed.
+  cudaGraphExec_t graph_for(int mode, int n, bool obs) {
+    auto key = std::make_tuple(mode, n, obs ? 1 : 0);
+    auto it = graphs.find(key);
+    if (it != graphs.end()) return it->second;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < n; ++k) {
+      if (mode == MODE_DST)
+        launch_step<MODE_DST>(obs && k == 0);
+      else
+        launch_step<MODE_ICG>(false);
+    }
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e));
+    graphs[key] = ge;
+    return ge;
+  }
+
+  // The device counter holds the step being executed; every step's first scan
+  // advances it, so it only needs setting when the host moves `step`.
+  void set_device_step() {
+    if (dev_next == step) return;
+    k_set_step<<<1, 1, 0, stream>>>(d_step.p, (unsigned long long)(step - 1));
+    CK(cudaGetLastError());
+    dev_next = step;
+  }
+
+  // n steps of the given mode; observation every obs_every steps (DST only).
+  void run_steps(uint64_t n, int mode, uint32_t obs_every) {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    set_device_step();
+    const int chunk = 128;
+    uint64_t left = n;
+    while (left > 0) {
+      int g;
+      bool obs = false;
+      if (mode == MODE_DST && obs_every > 0) {
+        uint64_t to_next = (obs_every - (step % obs_every)) % obs_every;
+        if (to_next == 0) {
+          obs = true;
+          g = (int)std::min<uint64_t>(left, obs_every);
+        } else {
+          g = (int)std::min<uint64_t>(left, to_next);
+        }
+        if (g > 4 * chunk) g = 4 * chunk;
+      } else {
+        g = (int)std::min<uint64_t>(left, chunk);
+      }
+      CK(cudaGraphLaunch(graph_for(mode, g, obs), stream));
+      if (obs) ++frames_observed;
+      step += g;
+      dev_next += g;
+      left -= g;
+    }
+  }
+
+  void sync_and_check() {
+    CK(cudaStreamSynchronize(stream));
+    int e[ERR_COUNT];
+    CK(cudaMemcpy(e, d_err.p, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e[ERR_NAN]) throw Error(ST_STATE, "non-finite bead position");
+    if (e[ERR_SLOT]) throw Error(ST_STATE, "cell list inconsistent with positions");
+  }
+
+  // Standalone analysis at the current positions.
+  void sort_now() {
+    launch_scan(false);
+    launch_scatter(pos.p);
+  }
+
+  void observe(bool with_sdist) {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    sort_now();
+    launch_observe_sorted(with_sdist);
+    recount();
+    CK(cudaGetLastError());
+    ++frames_observed;
+    sync_and_check();
+  }
+
+  void reset_observables() {
+    CK(cudaMemsetAsync(map.p, 0, sizeof(int32_t) * std::max<int64_t>(map_total, 1), stream));
+    CK(cudaMemsetAsync(ps.p, 0, sizeof(int32_t) * std::max(ps_total, 1), stream));
+    CK(cudaMemsetAsync(ds.p, 0, sizeof(double) * std::max(ps_total, 1), stream));
+    CK(cudaMemsetAsync(obs.p, 0, sizeof(double) * hsys.size() * OBS_STRIDE, stream));
+    frames_observed = 0;
+  }
+
+  std::vector<unsigned long long> overlaps() {
+    CK(cudaMemsetAsync(ovl.p, 0, sizeof(unsigned long long) * hsys.size(), stream));
+    sort_now();
+    k_contacts<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p, start.p,
+                                                              contact_args(false, false, true));
+    recount();
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> o(hsys.size());
+    CK(cudaMemcpyAsync(o.data(), ovl.p, sizeof(unsigned long long) * o.size(),
+                       cudaMemcpyDeviceToHost, stream));
+    sync_and_check();
+    return o;
+  }
+
+  std::vector<float> forces() {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    sort_now();
+    launch_pair<MODE_DST>();
+    k_total_force<MODE_DST><<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+        d_tiles.p, d_sys.p, ff, pos.p, fs.p, rank.p, start.p, lbs_sorted.p, lbs_start.p, fout.p);
+    recount();
+    CK(cudaGetLastError());
+    k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(fout.p, xyz_stage.p, nb);
+    std::vector<float> f((size_t)3 * nb);
+    CK(cudaMemcpyAsync(f.data(), xyz_stage.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost,
+                       stream));
+    sync_and_check();
+    return f;
+  }
+
+  // -------------------------------------------------------------- init
+  void generate_initial_condition() {
+    for (size_t s = 0; s < hsys.size(); ++s) {
+      const SysDesc &d = hsys[s];
+      const SystemSpec &q = specs[s];
+      HostRng rng(q.seed, 0x51u);
+      std::vector<float> l;
+      place_lbs(geo[s], ff.lbs_depth, ff.lco, d.n_lbs, rng, l);
+      std::copy(l.begin(), l.end(), hlbs.begin() + 3 * (size_t)d.lbs_off);
+      std::vector<int32_t> pt;
+      if (par.preset == PRESET_CCP)
+        make_types_ccp((uint32_t)d.n, par.sequence_file, rng, pt);
+      else
+        make_types_markov(d.n, par.mean_block, par.lad_fraction, rng, pt);
+      std::copy(pt.begin(), pt.end(), hpt.begin() + d.bead_off);
+      std::vector<int> heads;
+      for (int c = 0; c < d.n_chains; ++c) heads.push_back(chain_first[d.chain_off + c] - d.bead_off);
+      bool diploid = par.preset == PRESET_CCP && (uint32_t)d.n == CCP_N_DEF && d.n_chains == 12;
+      std::vector<float> x;
+      random_walk(geo[s], ff, diploid, heads, d.n, rng, x);
+      std::copy(x.begin(), x.end(), hxyz.begin() + 3 * (size_t)d.bead_off);
+    }
+    upload_lbs();
+    upload_positions();
+    relax();
+    download_positions();
+  }
+
+  // Soft-repulsion relaxation until no non-bonded pair overlaps
+  // (chrsim.cu:492-518); rounds of spf steps.
+  void relax() {
+    for (int round = 0; round < 10000; ++round) {
+      auto o = overlaps();
+      unsigned long long tot = 0;
+      for (auto v : o) tot += v;
+      if (tot == 0) return;
+      uint64_t saved = step;
+      run_steps(par.spf, MODE_ICG, 0);
+      step = saved;  // relaxation does not advance simulated time
+      sync_and_check();
+    }
+    throw Error(ST_STATE, "initial condition relaxation did not converge");
+  }
+
+  // -------------------------------------------------------------- frames
+  // chrsim::run_simulation: fpf frames of spf steps; frame k's positions are
+  // copied while frame k+1 runs.
+  void run_simulation(ccpgpu_frame_fn fn, void *user) {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    const SysDesc &d0 = hsys[0];
+    int pending = -1;
+    uint32_t pend_if = 0;
+    float pend_t = 0;
+    for (uint32_t ffi = 0; ffi < par.fpf; ++ffi) {
+      run_steps(par.spf, MODE_DST, 0);
+      int b = ffi & 1;
+      k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(pos.p, xyz_stage.p, nb);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(pinned[b], xyz_stage.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost,
+                         stream));
+      CK(cudaEventRecord(ev[b], stream));
+      for (auto &v : i_f) ++v;
+      for (auto &v : t) v += par.spf * ff.dt;
+      if (pending >= 0) {
+        CK(cudaEventSynchronize(ev[pending]));
+        if (fn && fn(user, pend_if, pend_t, pinned[pending] + 3 * (size_t)d0.bead_off, d0.n))
+          throw Error(ST_IO, "frame callback failed");
+      }
+      pending = b;
+      pend_if = i_f[0];
+      pend_t = t[0];
+    }
+    if (pending >= 0) {
+      CK(cudaEventSynchronize(ev[pending]));
+      if (fn && fn(user, pend_if, pend_t, pinned[pending] + 3 * (size_t)d0.bead_off, d0.n))
+        throw Error(ST_IO, "frame callback failed");
+      std::memcpy(hxyz.data(), pinned[pending], sizeof(float) * 3 * nb);
+    }
+    sync_and_check();
+  }
+};
+
+// ------------------------------------------------------------------ helpers
+
+static std::vector<SystemSpec> single_spec(const Params &p, uint64_t seed) {
+  SystemSpec s;
+  s.n = (int)p.N;
+  s.R_n = p.R_n;
+  s.R_o = p.R_o;
+  s.R_b = p.R_b;
+  s.n_lbs = (int)p.n_l;
+  s.seed = seed;
+  s.contact_bins = p.contact_bins;
+  if (p.preset == PRESET_CCP && p.N == CCP_N_DEF && p.n_chains == 12) {
+    for (int c = 0; c < 12; ++c) s.chain_first.push_back((int)CCP_CHR_LIM[c]);
+    s.n_chains = 12;
+  } else {
+    s.n_chains = p.n_chains;
+  }
+  return {s};
+}
+
+}  // namespace ccpgpu
+
+using namespace ccpgpu;
+
+struct ccpgpu_sim {
+  std::unique_ptr<Engine> e;
+};
+
+static thread_local std::string g_last_error;
+
+template <typename F>
+static int guarded(F &&f) {
+  try {
+    f();
+    return CCPGPU_OK;
+  } catch (const Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "out of host memory";
+    return CCPGPU_ERR_ARG;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return CCPGPU_ERR_ARG;
+  }
+}
+
+static void need(bool c, const char *m) {
+  if (!c) throw Error(ST_ARG, m);
+}
+
+static int put_bytes(const std::string &s, void *buf, size_t cap, size_t *len) {
+  if (len) *len = s.size();
+  if (!buf || cap < s.size()) {
+    g_last_error = "buffer too small";
+    return CCPGPU_ERR_IO;
+  }
+  std::memcpy(buf, s.data(), s.size());
+  return CCPGPU_OK;
+}
+
+extern "C" {
+
+const char *ccpgpu_last_error(void) { return g_last_error.c_str(); }
+
+int ccpgpu_create(const char *param_text, uint64_t seed, ccpgpu_sim **out) {
+  return guarded([&] {
+    need(param_text && out, "null argument");
+    *out = nullptr;
+    Params p = parse_params(param_text);
+    uint64_t sd = ParamMap(param_text).has("seed") ? p.seed : seed;
+    auto h = std::make_unique<ccpgpu_sim>();
+    h->e = std::make_unique<Engine>();
+    h->e->build(p, single_spec(p, sd));
+    *out = h.release();
+  });
+}
+
+int ccpgpu_batch_create(const char *param_text, int32_t n_systems, const int32_t *n_beads,
+                        const int32_t *n_chains, const float *radii, const uint64_t *seeds,
+                        uint64_t seed, ccpgpu_sim **out) {
+  return guarded([&] {
+    need(param_text && out && n_beads && n_systems > 0, "null argument");
+    *out = nullptr;
+    Params p = parse_params(param_text);
+    ParamMap pm(param_text);
+    std::vector<SystemSpec> sp(n_systems);
+    for (int s = 0; s < n_systems; ++s) {
+      SystemSpec &q = sp[s];
+      q.n = n_beads[s];
+      need(q.n >= 3, "system with fewer than 3 beads");
+      q.n_chains = n_chains ? n_chains[s] : 1;
+      need(q.n_chains >= 1 && q.n_chains <= q.n, "bad chain count");
+      if (radii)
+        q.R_n = radii[s];
+      else if (pm.has("nucleus_radius"))
+        q.R_n = p.R_n;
+      else
+        q.R_n = (float)(0.5 * std::cbrt((double)q.n / p.packing_fraction));
+      need(q.R_n > 1.0f, "nucleus radius too small");
+      q.R_o = 0.0f;
+      q.R_b = 0.0f;
+      Geometry g = make_geometry(q.R_n, q.R_o, q.R_b);
+      if (pm.has("number_of_lbs")) {
+        q.n_lbs = (int)p.n_l;
+      } else if (p.preset == PRESET_BASELINE) {
+        float noacf = 2.0f / (1.0f + g.noc);
+        q.n_lbs = (int)std::floor(p.lbs_area_fraction * 4.0 /
+                                  std::pow(p.ff.lco / (q.R_n - p.ff.lbs_depth), 2.0) * noacf);
+      } else {
+        q.n_lbs = 0;
+      }
+      q.seed = seeds ? seeds[s] : (seed + (uint64_t)s);
+      q.contact_bins = p.contact_bins;
+    }
+    auto h = std::make_unique<ccpgpu_sim>();
+    h->e = std::make_unique<Engine>();
+    h->e->build(p, std::move(sp));
+    *out = h.release();
+  });
+}
+
+int ccpgpu_destroy(ccpgpu_sim *h) {
+  return guarded([&] { delete h; });
+}
+
+int ccpgpu_info_get(const ccpgpu_sim *h, ccpgpu_info *o) {
+  return guarded([&] {
+    need(h && o, "null argument");
+    const Engine &e = *h->e;
+    std::memset(o, 0, sizeof(*o));
+    o->n_systems = (int32_t)e.hsys.size();
+    o->n_beads = e.nb;
+    o->n_lbs = e.nl;
+    o->n_chains = e.nch;
+    o->n_cells = e.nc;
+    o->preset = e.par.preset;
+    o->frames_per_file = e.par.fpf;
+    o->steps_per_frame = e.par.spf;
+    o->frame_index = e.i_f[0];
+    o->time = e.t[0];
+    o->step = e.step;
+    o->dt = e.ff.dt;
+    o->kT = e.ff.kT;
+    o->noise_sd = e.ff.sd;
+    o->contact_cutoff = e.par.contact_cutoff;
+    o->frames_observed = e.frames_observed;
+  });
+}
+
+int ccpgpu_system_info_get(const ccpgpu_sim *h, int32_t sys, ccpgpu_system_info *o) {
+  return guarded([&] {
+    need(h && o, "null argument");
+    const Engine &e = *h->e;
+    need(sys >= 0 && sys < (int)e.hsys.size(), "system index out of range");
+    const SysDesc &d = e.hsys[sys];
+    std::memset(o, 0, sizeof(*o));
+    o->bead_offset = d.bead_off;
+    o->n_beads = d.n;
+    o->chain_offset = d.chain_off;
+    o->n_chains = d.n_chains;
+    o->lbs_offset = d.lbs_off;
+    o->n_lbs = d.n_lbs;
+    o->cells_per_side = d.cps;
+    o->cell_side = d.csl;
+    o->nucleus_radius = d.R_n;
+    o->opening_radius = d.R_o;
+    o->bleb_radius = d.R_b;
+    o->contact_bins = d.nbins;
+    o->map_len = d.map_len;
+    o->copy_len = d.copy_len;
+    o->n_copies = d.n_copies;
+    o->map_offset = d.map_off;
+    o->seed = e.specs[sys].seed;
+  });
+}
+
+int ccpgpu_generate_initial_condition(ccpgpu_sim *h) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->generate_initial_condition();
+  });
+}
+
+int ccpgpu_run_simulation(ccpgpu_sim *h, ccpgpu_frame_fn fn, void *user) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->run_simulation(fn, user);
+  });
+}
+
+int ccpgpu_run_steps(ccpgpu_sim *h, uint64_t n_steps, uint32_t observe_every) {
+  return guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    e.run_steps(n_steps, MODE_DST, observe_every);
+    e.sync_and_check();
+    e.download_positions();
+  });
+}
+
+int ccpgpu_error_flags(ccpgpu_sim *h, int32_t *flags8, int32_t clear) {
+  return guarded([&] {
+    need(h && flags8, "null argument");
+    Engine &e = *h->e;
+    CK(cudaStreamSynchronize(e.stream));
+    CK(cudaMemcpy(flags8, e.d_err.p, sizeof(int) * ERR_COUNT, cudaMemcpyDeviceToHost));
+    if (clear) CK(cudaMemset(e.d_err.p, 0, sizeof(int) * ERR_COUNT));
+    if (flags8[ERR_NAN] || flags8[ERR_SLOT]) throw Error(ST_STATE, "device error flag set");
+  });
+}
+
+int ccpgpu_get_positions(ccpgpu_sim *h, float *xyz, size_t n) {
+  return guarded([&] {
+    need(h && xyz, "null argument");
+    Engine &e = *h->e;
+    need(n >= (size_t)3 * e.nb, "buffer too small");
+    if (e.positions_valid) e.download_positions();
+    std::memcpy(xyz, e.hxyz.data(), sizeof(float) * 3 * e.nb);
+  });
+}
+
+int ccpgpu_set_positions(ccpgpu_sim *h, const float *xyz, size_t n) {
+  return guarded([&] {
+    need(h && xyz, "null argument");
+    Engine &e = *h->e;
+    need(n >= (size_t)3 * e.nb, "buffer too small");
+    std::memcpy(e.hxyz.data(), xyz, sizeof(float) * 3 * e.nb);
+    e.upload_lbs();
+    e.upload_positions();
+  });
+}
+
+int ccpgpu_get_types(const ccpgpu_sim *h, int32_t *pt, size_t n) {
+  return guarded([&] {
+    need(h && pt, "null argument");
+    need(n >= (size_t)h->e->nb, "buffer too small");
+    std::memcpy(pt, h->e->hpt.data(), 4 * (size_t)h->e->nb);
+  });
+}
+
+int ccpgpu_set_types(ccpgpu_sim *h, const int32_t *pt, size_t n) {
+  return guarded([&] {
+    need(h && pt, "null argument");
+    Engine &e = *h->e;
+    need(n >= (size_t)e.nb, "buffer too small");
+    std::memcpy(e.hpt.data(), pt, 4 * (size_t)e.nb);
+    if (e.positions_valid) {
+      e.download_positions();
+      e.upload_positions();
+    }
+  });
+}
+
+int ccpgpu_get_lbs(const ccpgpu_sim *h, float *xyz, size_t n) {
+  return guarded([&] {
+    need(h && (xyz || h->e->nl == 0), "null argument");
+    need(n >= (size_t)3 * h->e->nl, "buffer too small");
+    if (h->e->nl) std::memcpy(xyz, h->e->hlbs.data(), sizeof(float) * 3 * h->e->nl);
+  });
+}
+
+int ccpgpu_set_lbs(ccpgpu_sim *h, const float *xyz, size_t n) {
+  return guarded([&] {
+    need(h && (xyz || h->e->nl == 0), "null argument");
+    Engine &e = *h->e;
+    need(n >= (size_t)3 * e.nl, "buffer too small");
+    if (e.nl) std::memcpy(e.hlbs.data(), xyz, sizeof(float) * 3 * e.nl);
+    e.upload_lbs();
+  });
+}
+
+int ccpgpu_compute_forces(ccpgpu_sim *h, float *f, size_t n) {
+  return guarded([&] {
+    need(h && f, "null argument");
+    Engine &e = *h->e;
+    need(n >= (size_t)3 * e.nb, "buffer too small");
+    auto v = e.forces();
+    std::memcpy(f, v.data(), sizeof(float) * 3 * e.nb);
+  });
+}
+
+static const SysDesc &sys_of(ccpgpu_sim *h, int32_t sys) {
+  need(sys >= 0 && sys < (int)h->e->hsys.size(), "system index out of range");
+  return h->e->hsys[sys];
+}
+
+int ccpgpu_frame_txt(ccpgpu_sim *h, int32_t sys, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    if (e.positions_valid) e.download_positions();
+    std::vector<int32_t> pt(e.hpt.begin() + d.bead_off, e.hpt.begin() + d.bead_off + d.n);
+    rc = put_bytes(format_frame_txt(e.i_f[sys], e.t[sys], pt, e.hxyz.data() + 3 * (size_t)d.bead_off,
+                                    d.n),
+                   buf, cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_lbs_txt(ccpgpu_sim *h, int32_t sys, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    rc = put_bytes(format_lbs_txt(e.hlbs.data() + 3 * (size_t)d.lbs_off, d.n_lbs), buf, cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_frame_trr(ccpgpu_sim *h, int32_t sys, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    if (e.positions_valid) e.download_positions();
+    rc = put_bytes(
+        format_trr_frame(e.i_f[sys], e.t[sys], e.hxyz.data() + 3 * (size_t)d.bead_off, d.n), buf,
+        cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_checkpoint(ccpgpu_sim *h, int32_t sys, void *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    if (e.positions_valid) e.download_positions();
+    std::vector<int32_t> pt(e.hpt.begin() + d.bead_off, e.hpt.begin() + d.bead_off + d.n);
+    rc = put_bytes(format_checkpoint(e.i_f[sys], e.t[sys], pt,
+                                     e.hxyz.data() + 3 * (size_t)d.bead_off, d.n,
+                                     e.hlbs.data() + 3 * (size_t)d.lbs_off, d.n_lbs),
+                   buf, cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_load_checkpoint(ccpgpu_sim *h, int32_t sys, const void *buf, size_t len) {
+  return guarded([&] {
+    need(h && buf, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    uint32_t i_f;
+    float t;
+    std::vector<int32_t> pt;
+    std::vector<float> x, l;
+    if (!parse_checkpoint(buf, len, d.n, d.n_lbs, i_f, t, pt, x, l))
+      throw Error(ST_IO, "failed to read checkpoint");
+    if (e.positions_valid) e.download_positions();
+    std::copy(pt.begin(), pt.end(), e.hpt.begin() + d.bead_off);
+    std::copy(x.begin(), x.end(), e.hxyz.begin() + 3 * (size_t)d.bead_off);
+    std::copy(l.begin(), l.end(), e.hlbs.begin() + 3 * (size_t)d.lbs_off);
+    e.i_f[sys] = i_f;
+    e.t[sys] = t;
+    // noise continues from the step implied by the frame index
+    e.step = (uint64_t)i_f * e.par.spf;
+    e.upload_lbs();
+    e.upload_positions();
+  });
+}
+
+int ccpgpu_read_frame_txt(ccpgpu_sim *h, int32_t sys, const char *text, size_t len) {
+  return guarded([&] {
+    need(h && text, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    uint32_t i_f;
+    float t;
+    std::vector<int32_t> pt;
+    std::vector<float> x;
+    if (!parse_frame_txt(std::string(text, len), d.n, i_f, t, pt, x))
+      throw Error(ST_IO, "failed to read frame from text file");
+    if (e.positions_valid) e.download_positions();
+    std::copy(pt.begin(), pt.end(), e.hpt.begin() + d.bead_off);
+    std::copy(x.begin(), x.end(), e.hxyz.begin() + 3 * (size_t)d.bead_off);
+    e.i_f[sys] = i_f;
+    e.t[sys] = t;
+    e.upload_lbs();
+    e.upload_positions();
+  });
+}
+
+int ccpgpu_read_lbs_txt(ccpgpu_sim *h, int32_t sys, const char *text, size_t len) {
+  return guarded([&] {
+    need(h && text, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    std::vector<float> l;
+    if (!parse_lbs_txt(std::string(text, len), d.n_lbs, l))
+      throw Error(ST_IO, "failed to read lamina binding sites from text file");
+    std::copy(l.begin(), l.end(), e.hlbs.begin() + 3 * (size_t)d.lbs_off);
+    e.upload_lbs();
+  });
+}
+
+int ccpgpu_observe(ccpgpu_sim *h, int32_t with_sdist) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->observe(with_sdist != 0);
+  });
+}
+
+int ccpgpu_reset_observables(ccpgpu_sim *h) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->reset_observables();
+    CK(cudaStreamSynchronize(h->e->stream));
+  });
+}
+
+int ccpgpu_contact_counts(ccpgpu_sim *h, int32_t sys, int32_t *tri, size_t n) {
+  return guarded([&] {
+    need(h && tri, "null argument");
+    Engine &e = *h->e;
+    const SysDesc &d = sys_of(h, sys);
+    size_t m = (size_t)d.nbins * (d.nbins + 1) / 2;
+    need(n >= m, "buffer too small");
+    CK(cudaStreamSynchronize(e.stream));
+    CK(cudaMemcpy(tri, e.map.p + d.map_off, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
+  });
+}
+
+int ccpgpu_observable_sums(ccpgpu_sim *h, int32_t sys, double *out, size_t n) {
+  return guarded([&] {
+    need(h && out, "null argument");
+    Engine &e = *h->e;
+    sys_of(h, sys);
+    need(n >= (size_t)OBS_STRIDE, "buffer too small");
+    CK(cudaStreamSynchronize(e.stream));
+    CK(cudaMemcpy(out, e.obs.p + (size_t)sys * OBS_STRIDE, sizeof(double) * OBS_STRIDE,
+                  cudaMemcpyDeviceToHost));
+  });
+}
+
+int ccpgpu_separation_counts(ccpgpu_sim *h, int32_t chain, int32_t *counts, double *dist,
+                             size_t n) {
+  return guarded([&] {
+    need(h, "null argument");
+    Engine &e = *h->e;
+    need(chain >= 0 && chain < e.nch, "chain index out of range");
+    size_t m = (size_t)e.chain_smax[chain] + 1;
+    need(n >= m, "buffer too small");
+    CK(cudaStreamSynchronize(e.stream));
+    if (counts)
+      CK(cudaMemcpy(counts, e.ps.p + e.chain_ps_off[chain], sizeof(int32_t) * m,
+                    cudaMemcpyDeviceToHost));
+    if (dist)
+      CK(cudaMemcpy(dist, e.ds.p + e.chain_ps_off[chain], sizeof(double) * m,
+                    cudaMemcpyDeviceToHost));
+  });
+}
+
+int ccpgpu_overlaps(ccpgpu_sim *h, uint64_t *per_system, size_t n) {
+  return guarded([&] {
+    need(h && per_system, "null argument");
+    Engine &e = *h->e;
+    need(n >= e.hsys.size(), "buffer too small");
+    auto o = e.overlaps();
+    for (size_t s = 0; s < o.size(); ++s) per_system[s] = o[s];
+  });
+}
+
+}  // extern "C"

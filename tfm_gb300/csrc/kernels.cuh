@@ -1,0 +1,812 @@
+// Device kernels of the GB300 Brownian-dynamics engine.
+//
+// One Heun step (ccp's stochastic Runge-Kutta, chrsim.cu:365-416) is
+//   [scan -> scatter(r) -> pair -> update<1>] [scan -> scatter(er) -> pair -> update<2>]
+// where
+//   scan     turns per-cell bead counts into cell start offsets (3 launches),
+//   scatter  writes every bead into cell order (the sorted float4 copy),
+//   pair     evaluates the excluded-volume / attraction forces over the
+//            27-cell neighbourhood in cell order (chrsim.cu:224-317),
+//   update   is the fused chain-order pass: bonded + bending (chrsim.cu:13-76),
+//            wall (chrsim.cu:79-170), lamina binding (chrsim.cu:202-212,
+//            261-273), counter-based noise (replaces chrsim.cu:336-361), the
+//            integrator stage, and the cell count of the new position (the
+//            histogram of the next counting sort, replacing sugrid.cu:15-77 and
+//            the CUB radix sort of sugrid.cu:130).
+// All kernels take a tile table: each CTA owns a contiguous bead range of one
+// system, so per-system geometry is uniform across a CTA.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ccpgpu {
+
+enum : int {
+  ERR_NAN = 0,       // non-finite position produced
+  ERR_ESCAPE = 1,    // bead outside its cell grid (clamped to the border)
+  ERR_SLOT = 2,      // scatter slot outside the system range (inconsistent counts)
+  ERR_NOISE = 3,     // truncated normal needed more than NOISE_MAX_ATTEMPTS draws
+  ERR_COUNT = 8,
+};
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;                       // cells per thread
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;  // cells per CTA
+constexpr int SCAN_TOP_THREADS = 1024;
+
+struct Tile {
+  int32_t sys;    // system index
+  int32_t begin;  // first bead (chain order) or slot (cell order) of the tile
+};
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ uint32_t wbits(float4 p) { return __float_as_uint(p.w); }
+
+// Integer cell coordinate along one axis of a grid centred at the origin with
+// cps cells per side (sugrid.cu:27-34 / chrsim.cu:292-293). Out-of-grid values
+// are clamped to the border cell and reported.
+__device__ __forceinline__ int cell_coord(float v, float inv_csl, int cps, bool &esc) {
+  float c = floorf(__fmul_rn(v, inv_csl)) + (float)(cps >> 1);
+  if (!(c >= 0.0f)) {
+    esc = true;
+    return 0;
+  }
+  if (c >= (float)cps) {
+    esc = true;
+    return cps - 1;
+  }
+  return (int)c;
+}
+
+struct CellXYZ {
+  int x, y, z;
+};
+
+__device__ __forceinline__ CellXYZ cell_of(float4 p, const SysDesc &s, bool &esc) {
+  CellXYZ c;
+  c.x = cell_coord(p.x, s.inv_csl, s.cps, esc);
+  c.y = cell_coord(p.y, s.inv_csl, s.cps, esc);
+  c.z = cell_coord(p.z, s.inv_csl, s.cps, esc);
+  return c;
+}
+
+__device__ __forceinline__ int cell_linear(CellXYZ c, const SysDesc &s) {
+  return s.cell_off + (c.z * s.cps + c.y) * s.cps + c.x;
+}
+
+__device__ __forceinline__ void set_err(int *err, int code) {
+  if (err[code] == 0) atomicExch(&err[code], 1);
+}
+
+// ---- well-conditioned FP32 building blocks
+// Error of the rounded sum s = a + b (TwoSum, Knuth): a + b = s + err exactly.
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  float t = __fsub_rn(s, a);
+  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, t)), __fsub_rn(b, t));
+}
+
+// a^2 + b^2 + c^2 - (kh + kl) from error-free products and sums: keeps full
+// relative precision when the squared length is close to kh (bond lengths near
+// l_0, beads near the wall), where the naive form cancels.
+__device__ __forceinline__ float sq3_minus(float a, float b, float c, float kh, float kl) {
+  float pa = __fmul_rn(a, a), ea = __fmaf_rn(a, a, -pa);
+  float pb = __fmul_rn(b, b), eb = __fmaf_rn(b, b, -pb);
+  float pc = __fmul_rn(c, c), ec = __fmaf_rn(c, c, -pc);
+  float s1 = __fadd_rn(pa, pb), e1 = two_sum_err(pa, pb, s1);
+  float s2 = __fadd_rn(s1, pc), e2 = two_sum_err(s1, pc, s2);
+  float s3 = __fsub_rn(s2, kh), e3 = two_sum_err(s2, -kh, s3);
+  float lo = __fadd_rn(__fadd_rn(__fadd_rn(ea, eb), __fadd_rn(ec, e1)),
+                       __fsub_rn(__fadd_rn(e2, e3), kl));
+  return __fadd_rn(s3, lo);
+}
+
+// R / d - 1 = (R^2 - d^2) / ((R + d) d) for the point (a, b, c) at distance d.
+__device__ __forceinline__ float r_over_d_minus1(float R, float a, float b, float c, float d) {
+  float rh = __fmul_rn(R, R), rl = __fmaf_rn(R, R, -rh);
+  return -sq3_minus(a, b, c, rh, rl) / ((R + d) * d);
+}
+
+// Wang-Frenkel (rc = 2) coefficient e (18 d^4 - 96 d^2 + 96) / d^8 in the
+// factored form 6 e (d^2 - 4)(3 d^2 - 4) / d^8 (roots at the cutoffs 2 and 2/sqrt(3)).
+__device__ __forceinline__ float wf_coef(float e, float d2) {
+  float i2 = 1.0f / d2, i4 = i2 * i2;
+  return 6.0f * e * (__fsub_rn(d2, 4.0f) * __fmaf_rn(3.0f, d2, -4.0f)) * (i4 * i4);
+}
+
+// Lennard-Jones coefficient 24 e (2 / d^14 - 1 / d^8) = 24 e d^-8 (2 d^-6 - 1).
+__device__ __forceinline__ float lj_coef(float e, float d2) {
+  float i2 = 1.0f / d2, i6 = i2 * i2 * i2;
+  return 24.0f * e * (i6 * i2) * __fmaf_rn(2.0f, i6, -1.0f);
+}
+
+// Coefficient c of a pair force F_i = c (r_i - r_j) (chrsim.cu:174-198).
+template <int MODE>
+__device__ __forceinline__ float pair_coef(float d2, bool hh, const ForceField &ff) {
+  if (MODE == MODE_ICG) {
+    // soft repulsion 128 (3 rco - 3 d) (chrsim.cu:189-198)
+    if (d2 > ff.rc_icg * ff.rc_icg) return 0.0f;
+    float d = sqrtf(d2);
+    return ff.k_icg * (3.0f * ff.rc_icg - 3.0f * d);
+  }
+  float rc = hh ? ff.rc_att : ff.rc_rep;
+  if (d2 > rc * rc) return 0.0f;
+  if (ff.pot == POT_WF) return wf_coef(ff.e_att, d2);
+  return lj_coef(hh ? ff.e_att : ff.e_rep, d2);
+}
+
+// Wall-particle vector of ccp's nucleus + opening + bleb geometry
+// (chrsim.cu:92-137); the ICG mode uses the bare sphere (chrsim.cu:148-163).
+// Returns false when the vector is not finite (no wall force, chrsim.cu:137).
+template <int MODE>
+__device__ __forceinline__ bool wall_vector(float3 r, const SysDesc &s, float3 &v) {
+  if (MODE == MODE_ICG) {
+    float d = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+    float k = -r_over_d_minus1(s.R_n, r.x, r.y, r.z, d);
+    v = make_float3(r.x * k, r.y * k, r.z * k);
+  } else if (r.z < s.nod) {
+    float d = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+    if (r.z / d < s.noc) {
+      float k = -r_over_d_minus1(s.R_n, r.x, r.y, r.z, d);
+      v = make_float3(r.x * k, r.y * k, r.z * k);
+    } else {
+      d = sqrtf(r.x * r.x + r.y * r.y);
+      float k = -r_over_d_minus1(s.R_o, r.x, r.y, 0.0f, d);
+      v = make_float3(r.x * k, r.y * k, r.z - s.nod);
+    }
+  } else {
+    float3 q = make_float3(r.x, r.y, r.z - (s.nod + s.bod));
+    float d = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
+    if (-q.z / d < s.boc) {
+      float k = -r_over_d_minus1(s.R_b, q.x, q.y, q.z, d);
+      v = make_float3(q.x * k, q.y * k, q.z * k);
+    } else {
+      d = sqrtf(q.x * q.x + q.y * q.y);
+      float k = -r_over_d_minus1(s.R_o, q.x, q.y, 0.0f, d);
+      v = make_float3(q.x * k, q.y * k, q.z + s.bod);
+    }
+  }
+  float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+  return isfinite(l);
+}
+
+// Wall force (chrsim.cu:79-88 for the Wang-Frenkel form).
+__device__ __forceinline__ float wall_coef(float3 v, const ForceField &ff) {
+  float d = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+  if (d > ff.rc_w) return 0.0f;
+  float d2 = d * d;
+  if (ff.pot == POT_WF) return wf_coef(ff.e_w, d2);
+  return lj_coef(ff.e_w, d2);
+}
+
+// Truncated standard normals for one bead and step: three Box-Muller normals
+// from one Philox block, redrawn with the next attempt counter while any
+// |z| > 5 (chrsim.cu:350-356 truncation on the component triple).
+__device__ __forceinline__ float3 bead_noise(uint32_t bead, uint64_t step, uint32_t k0,
+                                             uint32_t k1, int *err) {
+  for (int a = 0; a < NOISE_MAX_ATTEMPTS; ++a) {
+    U32x4 b = noise_bits(bead, (uint32_t)a, step, k0, k1);
+    float r0 = sqrtf(-2.0f * logf(u01_open0(b.x)));
+    float s0, c0;
+    sincospif(2.0f * u01_open1(b.y), &s0, &c0);
+    float r1 = sqrtf(-2.0f * logf(u01_open0(b.z)));
+    float c1 = cospif(2.0f * u01_open1(b.w));
+    float3 z = make_float3(r0 * c0, r0 * s0, r1 * c1);
+    if (fabsf(z.x) <= NOISE_TRUNC && fabsf(z.y) <= NOISE_TRUNC && fabsf(z.z) <= NOISE_TRUNC)
+      return z;
+  }
+  set_err(err, ERR_NOISE);
+  return make_float3(0.0f, 0.0f, 0.0f);
+}
+
+// ------------------------------------------------------------------ count
+
+// Cell histogram of the current positions: rank[i] = position of bead i in
+// its cell, counts[c] += 1. Used after positions are (re)loaded; during
+// stepping the update kernel does this for the position it writes.
+__global__ void k_count(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                        const float4 *__restrict__ pos, uint32_t *__restrict__ counts,
+                        uint32_t *__restrict__ rank, int *__restrict__ err) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int i = t.begin + threadIdx.x;
+  if (i >= s.bead_off + s.n) return;
+  bool esc = false;
+  float4 p = pos[i];
+  int c = cell_linear(cell_of(p, s, esc), s);
+  rank[i] = atomicAdd(&counts[c], 1u);
+  if (esc) set_err(err, ERR_ESCAPE);
+}
+
+// ------------------------------------------------------------------ scan
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += n;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+template <int NT>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t wsum[NT / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = warp_incl_scan(v);
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = (lane < NT / 32) ? wsum[lane] : 0u;
+    uint32_t wi = warp_incl_scan(w);
+    if (lane < NT / 32) wsum[lane] = wi - w;
+    if (lane == NT / 32 - 1) *total = wi;
+  }
+  __syncthreads();
+  uint32_t r = wsum[wid] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+// Phase 1: per-CTA totals of SCAN_CHUNK cells. counts is padded to a multiple
+// of SCAN_CHUNK (zeros beyond n_cells).
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_reduce(const uint32_t *__restrict__ counts, uint32_t *__restrict__ block_sums) {
+  const uint4 *c4 = reinterpret_cast<const uint4 *>(counts) +
+                    (size_t)blockIdx.x * (SCAN_CHUNK / 4) + threadIdx.x * (SCAN_ITEMS / 4);
+  uint32_t v = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
+    uint4 q = c4[k];
+    v += q.x + q.y + q.z + q.w;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __shared__ uint32_t ws[SCAN_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < SCAN_THREADS / 32; ++w) t += ws[w];
+    block_sums[blockIdx.x] = t;
+  }
+}
+
+// Phase 2: one CTA scans the CTA totals in place (exclusive) and stores the
+// grand total at block_sums[nb]. It also advances the step counter when the
+// scan opens a new Heun step (bump != 0).
+__global__ void __launch_bounds__(SCAN_TOP_THREADS)
+    k_scan_top(uint32_t *__restrict__ block_sums, int nb, unsigned long long *step, int bump) {
+  __shared__ uint32_t tot;
+  uint32_t carry = 0;
+  for (int b0 = 0; b0 < nb; b0 += SCAN_TOP_THREADS) {
+    int i = b0 + threadIdx.x;
+    uint32_t v = (i < nb) ? block_sums[i] : 0u;
+    uint32_t ex = block_excl_scan<SCAN_TOP_THREADS>(v, &tot);
+    if (i < nb) block_sums[i] = carry + ex;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    block_sums[nb] = carry;
+    if (bump) *step += 1ull;
+  }
+}
+
+// Phase 3: cell start offsets (exclusive scan), start[n_cells] = total, and
+// the counts are cleared for the next histogram.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_apply(uint32_t *__restrict__ counts, const uint32_t *__restrict__ block_sums,
+                 uint32_t *__restrict__ start, int n_cells, int nb) {
+  uint4 *c4 = reinterpret_cast<uint4 *>(counts) + (size_t)blockIdx.x * (SCAN_CHUNK / 4) +
+              threadIdx.x * (SCAN_ITEMS / 4);
+  uint32_t v[SCAN_ITEMS];
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
+    uint4 q = c4[k];
+    v[4 * k + 0] = q.x;
+    v[4 * k + 1] = q.y;
+    v[4 * k + 2] = q.z;
+    v[4 * k + 3] = q.w;
+    c4[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  uint32_t tsum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    uint32_t x = v[k];
+    v[k] = tsum;
+    tsum += x;
+  }
+  __shared__ uint32_t tot;
+  uint32_t off = block_excl_scan<SCAN_THREADS>(tsum, &tot) + block_sums[blockIdx.x];
+  uint4 *s4 = reinterpret_cast<uint4 *>(start) + (size_t)blockIdx.x * (SCAN_CHUNK / 4) +
+              threadIdx.x * (SCAN_ITEMS / 4);
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS / 4; ++k)
+    s4[k] = make_uint4(off + v[4 * k], off + v[4 * k + 1], off + v[4 * k + 2], off + v[4 * k + 3]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) start[n_cells] = block_sums[nb];
+}
+
+// ------------------------------------------------------------------ scatter
+
+// Counting-sort scatter: bead i goes to slot start[cell] + rank[i] of the
+// cell-ordered copy, with its global index packed above the flag bits.
+__global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                          const float4 *__restrict__ src, const uint32_t *__restrict__ rank,
+                          const uint32_t *__restrict__ start, float4 *__restrict__ sorted,
+                          int *__restrict__ err) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int i = t.begin + threadIdx.x;
+  int end = s.bead_off + s.n;
+  if (i >= end) return;
+  bool esc = false;
+  float4 p = src[i];
+  int c = cell_linear(cell_of(p, s, esc), s);
+  uint32_t slot = start[c] + rank[i];
+  if (slot < (uint32_t)s.bead_off || slot >= (uint32_t)end) {
+    set_err(err, ERR_SLOT);
+    return;
+  }
+  uint32_t w = ((uint32_t)i << BF_BITS) | (wbits(p) & 7u);
+  sorted[slot] = make_float4(p.x, p.y, p.z, __uint_as_float(w));
+}
+
+// ------------------------------------------------------------------ pair
+
+// Excluded-volume and A-A attraction forces in cell order. Each thread owns
+// one sorted bead; for every (dy, dz) row of the 3x3x3 neighbourhood the three
+// x-adjacent cells form one contiguous range of the sorted array. Pairs with
+// |i - j| <= 1 are skipped, also across chain ends (chrsim.cu:250).
+template <int MODE>
+__global__ void __launch_bounds__(128)
+    k_pair(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
+           const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+           float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int slot = t.begin + threadIdx.x;
+  if (slot >= s.bead_off + s.n) return;
+  float4 p = sorted[slot];
+  uint32_t wi = wbits(p);
+  int gi = (int)(wi >> BF_BITS);
+  bool het = (wi & BF_HET) != 0u;
+  bool esc = false;
+  CellXYZ c = cell_of(p, s, esc);
+  const int cps = s.cps;
+  int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
+  float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+  for (int z = max(c.z - 1, 0); z <= min(c.z + 1, cps - 1); ++z) {
+    for (int y = max(c.y - 1, 0); y <= min(c.y + 1, cps - 1); ++y) {
+      int row = s.cell_off + (z * cps + y) * cps;
+      uint32_t b = __ldg(&start[row + x0]);
+      uint32_t e = __ldg(&start[row + x1 + 1]);
+      for (uint32_t k = b; k < e; ++k) {
+        float4 q = __ldg(&sorted[k]);
+        uint32_t wj = wbits(q);
+        int gj = (int)(wj >> BF_BITS);
+        if (abs(gi - gj) <= 1) continue;
+        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        float d2 = dx * dx + dy * dy + dz * dz;
+        float cf = pair_coef<MODE>(d2, het && (wj & BF_HET), ff);
+        fx += cf * dx;
+        fy += cf * dy;
+        fz += cf * dz;
+      }
+    }
+  }
+  fs[slot] = make_float4(fx, fy, fz, 0.0f);
+}
+
+// ------------------------------------------------------------------ update
+
+// Lamina-binding force on a LAD bead at x (chrsim.cu:202-212, 261-273): sites
+// within lco; only cells overlapping [x - lco, x + lco] are visited.
+__device__ __forceinline__ float3 lbs_force(float4 x, const SysDesc &s, const ForceField &ff,
+                                            const float4 *__restrict__ lbs,
+                                            const uint32_t *__restrict__ lbs_start) {
+  float3 f = make_float3(0.0f, 0.0f, 0.0f);
+  float d = sqrtf(x.x * x.x + x.y * x.y + x.z * x.z);
+  float rl = s.R_n - ff.lbs_depth;
+  if (fabsf(d - rl) > ff.lco * 1.001f + 1e-3f) return f;
+  float m = ff.lco * 1.001f + 1e-4f;
+  bool esc = false;
+  int xl = cell_coord(x.x - m, s.inv_csl, s.cps, esc), xh = cell_coord(x.x + m, s.inv_csl, s.cps, esc);
+  int yl = cell_coord(x.y - m, s.inv_csl, s.cps, esc), yh = cell_coord(x.y + m, s.inv_csl, s.cps, esc);
+  int zl = cell_coord(x.z - m, s.inv_csl, s.cps, esc), zh = cell_coord(x.z + m, s.inv_csl, s.cps, esc);
+  const float cl = ff.e_l * (8.0f / (3.0f * ff.lco * ff.lco));
+  for (int z = zl; z <= zh; ++z)
+    for (int y = yl; y <= yh; ++y) {
+      int row = s.cell_off + (z * s.cps + y) * s.cps;
+      uint32_t b = lbs_start[row + xl], e = lbs_start[row + xh + 1];
+      for (uint32_t k = b; k < e; ++k) {
+        float4 q = lbs[k];
+        float vx = x.x - q.x, vy = x.y - q.y, vz = x.z - q.z;
+        float dl = sqrtf(vx * vx + vy * vy + vz * vz);
+        if (dl > ff.lco) continue;
+        float nd = dl / ff.lco;
+        float n2 = nd * nd;
+        float cf = cl * (n2 * n2 * n2 - 1.0f);
+        f.x += cf * vx;
+        f.y += cf * vy;
+        f.z += cf * vz;
+      }
+    }
+  return f;
+}
+
+// Bonded (elastic + bending) force on bead i of X (chrsim.cu:13-76). Bonds
+// exist only inside a chain; BF_START marks chain heads.
+__device__ __forceinline__ float3 bonded_force(const float4 *__restrict__ X, int i, float4 xi,
+                                               int end, const ForceField &ff) {
+  uint32_t fi = wbits(xi);
+  float4 xm1 = xi, xm2 = xi, xp1 = xi, xp2 = xi;
+  bool e1 = (fi & BF_START) == 0u;  // bond (i-1, i)
+  bool e0 = false, e2 = false, e3 = false;
+  if (e1) {
+    xm1 = X[i - 1];
+    e0 = (wbits(xm1) & BF_START) == 0u;  // bond (i-2, i-1)
+    if (e0) xm2 = X[i - 2];
+  }
+  if (i + 1 < end) {
+    xp1 = X[i + 1];
+    e2 = (wbits(xp1) & BF_START) == 0u;  // bond (i, i+1)
+    if (e2 && i + 2 < end) {
+      xp2 = X[i + 2];
+      e3 = (wbits(xp2) & BF_START) == 0u;  // bond (i+1, i+2)
+    }
+  }
+  float3 v0 = e0 ? make_float3(xm1.x - xm2.x, xm1.y - xm2.y, xm1.z - xm2.z) : make_float3(0, 0, 0);
+  float3 v1 = e1 ? make_float3(xi.x - xm1.x, xi.y - xm1.y, xi.z - xm1.z) : make_float3(0, 0, 0);
+  float3 v2 = e2 ? make_float3(xp1.x - xi.x, xp1.y - xi.y, xp1.z - xi.z) : make_float3(0, 0, 0);
+  float3 v3 = e3 ? make_float3(xp2.x - xp1.x, xp2.y - xp1.y, xp2.z - xp1.z) : make_float3(0, 0, 0);
+  float il0 = e0 ? rsqrtf(v0.x * v0.x + v0.y * v0.y + v0.z * v0.z) : 0.0f;
+  float il1 = e1 ? rsqrtf(v1.x * v1.x + v1.y * v1.y + v1.z * v1.z) : 0.0f;
+  float il2 = e2 ? rsqrtf(v2.x * v2.x + v2.y * v2.y + v2.z * v2.z) : 0.0f;
+  float il3 = e3 ? rsqrtf(v3.x * v3.x + v3.y * v3.y + v3.z * v3.z) : 0.0f;
+  // k_e (1 - l_0 / d) = k_e (d^2 - l_0^2) / ((d + l_0) d), with d^2 - l_0^2 formed
+  // from the exact bond vector (rounded difference + its TwoSum residual)
+  float lh = __fmul_rn(ff.l_0, ff.l_0), ll = __fmaf_rn(ff.l_0, ff.l_0, -lh);
+  float ke1 = 0.0f, ke2 = 0.0f;
+  if (e1) {
+    float cx = v1.x * two_sum_err(xi.x, -xm1.x, v1.x) + v1.y * two_sum_err(xi.y, -xm1.y, v1.y) +
+               v1.z * two_sum_err(xi.z, -xm1.z, v1.z);
+    float s1 = __fadd_rn(sq3_minus(v1.x, v1.y, v1.z, lh, ll), 2.0f * cx);
+    float d1 = sqrtf(v1.x * v1.x + v1.y * v1.y + v1.z * v1.z);
+    ke1 = ff.k_e * (s1 / (d1 + ff.l_0)) * il1;
+  }
+  if (e2) {
+    float cx = v2.x * two_sum_err(xp1.x, -xi.x, v2.x) + v2.y * two_sum_err(xp1.y, -xi.y, v2.y) +
+               v2.z * two_sum_err(xp1.z, -xi.z, v2.z);
+    float s2 = __fadd_rn(sq3_minus(v2.x, v2.y, v2.z, lh, ll), 2.0f * cx);
+    float d2 = sqrtf(v2.x * v2.x + v2.y * v2.y + v2.z * v2.z);
+    ke2 = ff.k_e * (s2 / (d2 + ff.l_0)) * il2;
+  }
+  float3 f = make_float3(ke2 * v2.x - ke1 * v1.x, ke2 * v2.y - ke1 * v1.y, ke2 * v2.z - ke1 * v1.z);
+  if (ff.bend_all || (fi & BF_HET)) {
+    float cos0 = (v1.x * v0.x + v1.y * v0.y + v1.z * v0.z) * il1 * il0;
+    float cos1 = (v2.x * v1.x + v2.y * v1.y + v2.z * v1.z) * il2 * il1;
+    float cos2 = (v3.x * v2.x + v3.y * v2.y + v3.z * v2.z) * il3 * il2;
+    float a0 = il1 * il0, a1 = il1 * il2, a3 = il2 * il3;
+    float i11 = il1 * il1, i22 = il2 * il2;
+    // four terms of d/dr_i [cos(theta_{i-1}) + cos(theta_i) + cos(theta_{i+1})]
+    float c_v0 = a0;
+    float c_v1 = -cos0 * i11 - cos1 * i11 - a1;
+    float c_v2 = a1 + cos1 * i22 + cos2 * i22;
+    float c_v3 = -a3;
+    f.x += ff.k_b * (c_v0 * v0.x + c_v1 * v1.x + c_v2 * v2.x + c_v3 * v3.x);
+    f.y += ff.k_b * (c_v0 * v0.y + c_v1 * v1.y + c_v2 * v2.y + c_v3 * v3.y);
+    f.z += ff.k_b * (c_v0 * v0.z + c_v1 * v1.z + c_v2 * v2.z + c_v3 * v3.z);
+  }
+  return f;
+}
+
+// Fused chain-order pass of one Heun stage.
+//   STAGE 1: X = r.  f = F(r);  er = r + f dt + sd z           (chrsim.cu:365-388)
+//   STAGE 2: X = er. ef = F(er); r = r + (f + ef) dt / 2 + sd z (chrsim.cu:392-416)
+// F = bonded + wall + LBS + pair (pair read from the cell-ordered result).
+// The written position is binned into the next counting sort.
+template <int STAGE, int MODE>
+__global__ void __launch_bounds__(128)
+    k_update(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
+             float4 *__restrict__ pos, float4 *__restrict__ er, float4 *__restrict__ fbuf,
+             const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
+             const uint32_t *__restrict__ start, uint32_t *__restrict__ counts,
+             const float4 *__restrict__ lbs, const uint32_t *__restrict__ lbs_start,
+             const unsigned long long *__restrict__ step, int *__restrict__ err) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int i = t.begin + threadIdx.x;
+  int end = s.bead_off + s.n;
+  if (i >= end) return;
+  const float4 *X = (STAGE == 1) ? pos : er;
+  float4 xi = X[i];
+  uint32_t fl = wbits(xi);
+
+  // pair force of this bead from the cell-ordered pass
+  bool esc = false;
+  int c_old = cell_linear(cell_of(xi, s, esc), s);
+  uint32_t slot = start[c_old] + rank[i];
+  float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end)
+    fp = fs[slot];
+  else
+    set_err(err, ERR_SLOT);
+  float3 F = make_float3(fp.x, fp.y, fp.z);
+
+  float3 fb = bonded_force(X, i, xi, end, ff);
+  F.x += fb.x;
+  F.y += fb.y;
+  F.z += fb.z;
+
+  float3 vw;
+  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
+    float cw = wall_coef(vw, ff);
+    F.x += cw * vw.x;
+    F.y += cw * vw.y;
+    F.z += cw * vw.z;
+  }
+  if (MODE == MODE_DST && (fl & BF_LAD) && s.n_lbs > 0) {
+    float3 fl3 = lbs_force(xi, s, ff, lbs, lbs_start);
+    F.x += fl3.x;
+    F.y += fl3.y;
+    F.z += fl3.z;
+  }
+
+  float3 rn = make_float3(0.0f, 0.0f, 0.0f);
+  if (MODE == MODE_DST && ff.sd > 0.0f) {
+    float3 z = bead_noise((uint32_t)(i - s.bead_off), *step, s.seed_lo, s.seed_hi, err);
+    rn = make_float3(ff.sd * z.x, ff.sd * z.y, ff.sd * z.z);
+  }
+
+  float4 out;
+  if (STAGE == 1) {
+    out = make_float4(xi.x + F.x * ff.dt + rn.x, xi.y + F.y * ff.dt + rn.y,
+                      xi.z + F.z * ff.dt + rn.z, xi.w);
+    er[i] = out;
+    fbuf[i] = make_float4(F.x, F.y, F.z, 0.0f);
+  } else {
+    float4 r = pos[i];
+    float4 f1 = fbuf[i];
+    float h = 0.5f * ff.dt;
+    out = make_float4(r.x + (f1.x + F.x) * h + rn.x, r.y + (f1.y + F.y) * h + rn.y,
+                      r.z + (f1.z + F.z) * h + rn.z, r.w);
+    pos[i] = out;
+  }
+  if (!(isfinite(out.x) && isfinite(out.y) && isfinite(out.z))) set_err(err, ERR_NAN);
+  bool esc2 = false;
+  int c_new = cell_linear(cell_of(out, s, esc2), s);
+  rank[i] = atomicAdd(&counts[c_new], 1u);
+  if (esc2) set_err(err, ERR_ESCAPE);
+}
+
+// ------------------------------------------------------------------ forces only
+
+// Total force at the current positions in chain order (for parity checks and
+// ccp's host force array): bonded + wall + LBS + pair.
+template <int MODE>
+__global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                              ForceField ff, const float4 *__restrict__ pos,
+                              const float4 *__restrict__ fs, const uint32_t *__restrict__ rank,
+                              const uint32_t *__restrict__ start, const float4 *__restrict__ lbs,
+                              const uint32_t *__restrict__ lbs_start, float4 *__restrict__ out) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int i = t.begin + threadIdx.x;
+  int end = s.bead_off + s.n;
+  if (i >= end) return;
+  float4 xi = pos[i];
+  bool esc = false;
+  int c = cell_linear(cell_of(xi, s, esc), s);
+  uint32_t slot = start[c] + rank[i];
+  float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end) fp = fs[slot];
+  float3 F = make_float3(fp.x, fp.y, fp.z);
+  float3 fb = bonded_force(pos, i, xi, end, ff);
+  F.x += fb.x;
+  F.y += fb.y;
+  F.z += fb.z;
+  float3 vw;
+  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
+    float cw = wall_coef(vw, ff);
+    F.x += cw * vw.x;
+    F.y += cw * vw.y;
+    F.z += cw * vw.z;
+  }
+  if (MODE == MODE_DST && (wbits(xi) & BF_LAD) && s.n_lbs > 0) {
+    float3 fl3 = lbs_force(xi, s, ff, lbs, lbs_start);
+    F.x += fl3.x;
+    F.y += fl3.y;
+    F.z += fl3.z;
+  }
+  out[i] = make_float4(F.x, F.y, F.z, 0.0f);
+}
+
+// ------------------------------------------------------------------ contacts
+
+// Contact predicate shared with the oracle: |r_i - r_j| < cutoff with the
+// squared length formed as fma(dz, dz, fma(dy, dy, dx * dx)) and a correctly
+// rounded square root, so that counts are bit-exact given identical positions.
+__device__ __forceinline__ bool in_contact(float4 a, float4 b, float cut) {
+  float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  return __fsqrt_rn(d2) < cut;
+}
+
+struct ContactArgs {
+  float cut;              // contact cutoff (aco = 2 in ccp, chrana.cu:75)
+  float mis;              // overlap distance (chrsim.cuh:20)
+  int do_map, do_ps, do_overlap;
+  int32_t *map;           // packed lower-triangular counts of all systems
+  int32_t *ps;            // per-chain contact counts by separation
+  const int32_t *chain_of;     // global chain index of every bead
+  const int32_t *chain_first;  // first bead of every chain
+  const int32_t *chain_ps_off; // offset of every chain in ps
+  const int32_t *chain_smax;   // largest separation recorded per chain
+  unsigned long long *overlaps;  // per-system overlap count
+};
+
+// One pass over unordered bead pairs (i < j) within the contact cutoff of the
+// cell-ordered copy: binned contact map (calc_cm, chrana.cu:48-84), per-chain
+// contact counts by separation (the cp part of calc_sd_cp, chrana.cu:13-45) and
+// the overlap count of the initial-condition relaxation (chrsim.cu:805-820).
+__global__ void __launch_bounds__(128)
+    k_contacts(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+               const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+               ContactArgs a) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int slot = t.begin + threadIdx.x;
+  unsigned long long novl = 0;
+  if (slot < s.bead_off + s.n) {
+    float4 p = sorted[slot];
+    int gi = (int)(wbits(p) >> BF_BITS);
+    int li = gi - s.bead_off;
+    int copy_i = li / s.copy_len, lc_i = li - copy_i * s.copy_len;
+    bool mapped_i = a.do_map && copy_i < s.n_copies && lc_i < s.map_len;
+    int bin_i = mapped_i ? (int)(((long long)lc_i * s.nbins) / s.map_len) : 0;
+    int ch_i = a.chain_of[gi];
+    float mis2 = a.mis;
+    bool esc = false;
+    CellXYZ c = cell_of(p, s, esc);
+    const int cps = s.cps;
+    int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
+    for (int z = max(c.z - 1, 0); z <= min(c.z + 1, cps - 1); ++z)
+      for (int y = max(c.y - 1, 0); y <= min(c.y + 1, cps - 1); ++y) {
+        int row = s.cell_off + (z * cps + y) * cps;
+        uint32_t b = start[row + x0], e = start[row + x1 + 1];
+        for (uint32_t k = b; k < e; ++k) {
+          float4 q = sorted[k];
+          int gj = (int)(wbits(q) >> BF_BITS);
+          if (gj <= gi) continue;
+          if (a.do_overlap && gj - gi >= 2 && in_contact(p, q, mis2)) ++novl;
+          if (!in_contact(p, q, a.cut)) continue;
+          if (mapped_i) {
+            int lj = gj - s.bead_off;
+            int copy_j = lj / s.copy_len, lc_j = lj - copy_j * s.copy_len;
+            if (copy_j == copy_i && lc_j < s.map_len) {
+              int bin_j = (int)(((long long)lc_j * s.nbins) / s.map_len);
+              int bx = max(bin_i, bin_j), by = min(bin_i, bin_j);
+              long long idx = s.map_off + (long long)bx * (bx + 1) / 2 + by;
+              atomicAdd(&a.map[idx], bx == by ? 2 : 1);
+            }
+          }
+          if (a.do_ps) {
+            int ch_j = a.chain_of[gj];
+            if (ch_j == ch_i) {
+              int sep = gj - gi;
+              if (sep <= a.chain_smax[ch_i]) atomicAdd(&a.ps[a.chain_ps_off[ch_i] + sep], 1);
+            }
+          }
+        }
+      }
+  }
+  if (a.do_overlap) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) novl += __shfl_xor_sync(0xffffffffu, novl, o);
+    if ((threadIdx.x & 31) == 0 && novl) atomicAdd(&a.overlaps[t.sys], novl);
+  }
+}
+
+// ------------------------------------------------------------------ observables
+
+constexpr int N_SHELLS = 64;  // radial bins (chrana.cuh:16)
+
+// Per-system FP64 accumulators: [0..2] sum r, [3] sum |r|^2, then 3 x 64 radial
+// density volumes (A, B, all) of chrana.cu:422-480.
+constexpr int OBS_STRIDE = 4 + 3 * N_SHELLS;
+
+__global__ void __launch_bounds__(128)
+    k_observe(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+              const float4 *__restrict__ pos, float bead_r, double *__restrict__ acc) {
+  __shared__ double sh[OBS_STRIDE];
+  __shared__ float rb[N_SHELLS];
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  for (int k = threadIdx.x; k < OBS_STRIDE; k += blockDim.x) sh[k] = 0.0;
+  for (int k = threadIdx.x; k < N_SHELLS; k += blockDim.x)
+    rb[k] = s.R_n * cbrtf((k + 1.0f) / N_SHELLS);
+  __syncthreads();
+  int i = t.begin + threadIdx.x;
+  if (i < s.bead_off + s.n) {
+    float4 p = pos[i];
+    bool het = (wbits(p) & BF_HET) != 0u;
+    double px = p.x, py = p.y, pz = p.z;
+    atomicAdd(&sh[0], px);
+    atomicAdd(&sh[1], py);
+    atomicAdd(&sh[2], pz);
+    atomicAdd(&sh[3], px * px + py * py + pz * pz);
+    float dr = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
+    const float a = bead_r;
+    const float vfull = (4.0f / 3.0f) * 3.14159265358979f * a * a * a;
+    float vprev = 0.0f;
+    for (int b = 0; b < N_SHELLS; ++b) {
+      float r = rb[b], v;
+      if (dr - a > r) {
+        v = 0.0f;
+      } else if (dr + a < r) {
+        v = vfull;
+      } else {
+        float ca = (dr * dr + a * a - r * r) / (2.0f * dr * a);
+        float cb = (r * r + dr * dr - a * a) / (2.0f * r * dr);
+        float va = (3.14159265358979f / 3.0f) * a * a * a * (2.0f + ca) * (1.0f - ca) * (1.0f - ca);
+        float vb = (3.14159265358979f / 3.0f) * r * r * r * (2.0f + cb) * (1.0f - cb) * (1.0f - cb);
+        v = va + vb;
+      }
+      float dv = v - vprev;
+      vprev = v;
+      if (dv != 0.0f) {
+        atomicAdd(&sh[4 + (het ? 0 : 1) * N_SHELLS + b], (double)dv);
+        atomicAdd(&sh[4 + 2 * N_SHELLS + b], (double)dv);
+      }
+      if (v == vfull && dr + a < r) break;  // all further shells contribute zero
+    }
+  }
+  __syncthreads();
+  double *dst = acc + (size_t)t.sys * OBS_STRIDE;
+  for (int k = threadIdx.x; k < OBS_STRIDE; k += blockDim.x)
+    if (sh[k] != 0.0) atomicAdd(&dst[k], sh[k]);
+}
+
+// Mean spatial distance by separation (the sd part of calc_sd_cp,
+// chrana.cu:13-45): ds[chain_ps_off + s] += sum_p |r_{p+s} - r_p| over a chunk
+// of p, FP32 distances accumulated in FP64.
+constexpr int SDIST_PCHUNK = 256;
+
+__global__ void __launch_bounds__(128)
+    k_sdist(const float4 *__restrict__ pos, const int32_t *__restrict__ chain_first,
+            const int32_t *__restrict__ chain_len, const int32_t *__restrict__ chain_ps_off,
+            const int32_t *__restrict__ chain_smax, int chain, double *__restrict__ ds) {
+  int first = chain_first[chain], L = chain_len[chain], smax = chain_smax[chain];
+  int sep = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int p0 = blockIdx.y * SDIST_PCHUNK;
+  if (sep > smax || p0 >= L - sep) return;
+  int p1 = min(p0 + SDIST_PCHUNK, L - sep);
+  float acc = 0.0f;
+  for (int p = p0; p < p1; ++p) {
+    float4 a = pos[first + p], b = pos[first + p + sep];
+    float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    acc += sqrtf(dx * dx + dy * dy + dz * dz);
+  }
+  atomicAdd(&ds[chain_ps_off[chain] + sep], (double)acc);
+}
+
+// Sets the device step counter (the first scan of the next step bumps it).
+__global__ void k_set_step(unsigned long long *step, unsigned long long v) { *step = v; }
+
+// Positions as packed xyz triples (the .trr / checkpoint layout).
+__global__ void k_pack_xyz(const float4 *__restrict__ pos, float *__restrict__ xyz, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pos[i];
+  xyz[3 * i + 0] = p.x;
+  xyz[3 * i + 1] = p.y;
+  xyz[3 * i + 2] = p.z;
+}
+
+}  // namespace ccpgpu
