@@ -95,11 +95,13 @@ void orc_noise(uint32_t bead, uint64_t step, uint32_t k0, uint32_t k1, double *z
 
 /* ------------------------------------------------------------ contact predicate */
 
-/* |a - b| < cut with d^2 = fma(dz, dz, fma(dy, dy, dx*dx)) in float and a
- * correctly rounded square root: the engine's predicate, bit for bit. */
+/* |a - b| < cut with d^2 = fma(dz, dz, fma(dx, dx, dy*dy)) in float and a
+ * correctly rounded square root: the rounding of the reference's compiled
+ * length(r[x] - r[y]) < aco in calc_cm (chrana.cu:72-73), established against
+ * its output on pairs within 4 ulps of the cutoff (tests/golden/ccp_cutoff.npz). */
 static int in_contact(const float *a, const float *b, float cut) {
   volatile float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
-  float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  float d2 = fmaf(dz, dz, fmaf(dx, dx, dy * dy));
   return sqrtf(d2) < cut;
 }
 

@@ -141,15 +141,18 @@ static inline SFX(v3) SFX(wall)(SFX(v3) r, const SFX(model) * m, int mode) {
 #undef ORC_RM1
   REAL d = SQRT(SFX(dot)(v, v));
   if (!isfinite(d)) return f;
-  if (d > m->rc_w) return f;
+  /* the relaxation wall is ccp's calc_wpf: Wang-Frenkel, eps = 1, cutoff rco */
+  int wf = (mode == MODE_ICG) || (m->pot == POT_WF);
+  REAL ew = (mode == MODE_ICG) ? 1 : m->e_w;
+  if (d > ((mode == MODE_ICG) ? (REAL)1.154701 : m->rc_w)) return f;
   REAL c;
-  if (m->pot == POT_WF) {
+  if (wf) {
     REAL d2 = d * d;
 #if ORC_ACCURATE
     REAL i2 = 1 / d2, i4 = i2 * i2;
-    c = m->e_w * 6 * ((d2 - 4) * fma((REAL)3, d2, (REAL)-4)) * (i4 * i4);
+    c = ew * 6 * ((d2 - 4) * fma((REAL)3, d2, (REAL)-4)) * (i4 * i4);
 #else
-    c = m->e_w * (18 * d2 * d2 - 96 * d2 + 96) / (d2 * d2 * d2 * d2);
+    c = ew * (18 * d2 * d2 - 96 * d2 + 96) / (d2 * d2 * d2 * d2);
 #endif
   } else {
     REAL i2 = 1 / (d * d), i6 = i2 * i2 * i2;

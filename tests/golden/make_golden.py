@@ -267,7 +267,10 @@ def near_cutoff_pairs(rng, n_pairs):
     """Bead pairs at |d| within a few ulps of the contact cutoff 2."""
     xyz = np.zeros((2 * n_pairs, 3), np.float32)
     for k in range(n_pairs):
-        base = (rng.random(3) * 160 - 80).astype(np.float32)
+        while True:
+            base = (rng.random(3) * 160 - 80).astype(np.float32)
+            if np.linalg.norm(base) < 95.0:
+                break
         u = rng.normal(size=3)
         u /= np.linalg.norm(u)
         t = 2.0 + (k % 9 - 4) * 2.4e-7

@@ -54,6 +54,7 @@ struct ForceField {
   float lbs_depth;  // LBS sit at R_n - lbs_depth
   float k_icg;      // soft repulsion of the ICG mode (128)
   float rc_icg;     // soft repulsion cutoff (rco)
+  float mis;        // relaxation ends when no non-bonded pair is closer (chrsim.cuh:20)
   float dt;         // time step
   float sd;         // noise standard deviation sqrt(2 kT dt)
   float kT;         // thermal energy
@@ -132,6 +133,10 @@ __host__ __device__ __forceinline__ float u01_open0(uint32_t x) {
 __host__ __device__ __forceinline__ float u01_open1(uint32_t x) {
   return (float)(x >> 8) * (1.0f / 16777216.0f);
 }
+
+// The relaxation (ICG) wall is ccp's Wang-Frenkel wall with eps = 1 and cutoff
+// rco for every preset (calc_cf<ICG>, chrsim.cu:148-170).
+constexpr float ICG_WALL_RC = 1.154701f;
 
 constexpr int NOISE_MAX_ATTEMPTS = 64;
 constexpr float NOISE_TRUNC = 5.0f;  // |z| <= 5 (chrsim.cu:356)

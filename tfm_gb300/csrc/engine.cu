@@ -359,7 +359,7 @@ struct Engine {
   ContactArgs contact_args(bool do_map, bool do_ps, bool do_ovl) {
     ContactArgs a;
     a.cut = par.contact_cutoff;
-    a.mis = CCP_MIS;
+    a.mis = ff.mis;
     a.do_map = do_map;
     a.do_ps = do_ps;
     a.do_overlap = do_ovl;

@@ -83,6 +83,7 @@ static ForceField preset_ccp(float T) {
   f.lbs_depth = CCP_RCO;
   f.k_icg = 128.0f;
   f.rc_icg = CCP_RCO;
+  f.mis = CCP_MIS;
   f.dt = (float)CCP_DT;
   f.kT = CCP_K_B * T;
   f.sd = (float)std::sqrt(2.0 * CCP_K_B * T * CCP_DT);  // chrsim.cu:424
@@ -108,6 +109,8 @@ static ForceField preset_baseline(float kT, float dt) {
   f.lbs_depth = wca;
   f.k_icg = 128.0f;
   f.rc_icg = CCP_RCO;
+  // WCA with dt = 1e-3 is stable (dt |dF/dr| < 2) only beyond r ~ 0.92
+  f.mis = 0.95f;
   f.dt = dt;
   f.kT = kT;
   f.sd = (float)std::sqrt(2.0 * (double)kT * (double)dt);
@@ -204,7 +207,7 @@ Params parse_params(const std::string &text) {
   if (p.contact_bins < 0) fail("contact_bins out of range");
   if (!(p.lad_fraction >= 0.0f && p.lad_fraction <= 1.0f)) fail("lad_fraction out of range");
   if (!(p.mean_block >= 1.0f)) fail("mean_block_length out of range");
-  float need = std::max({p.ff.rc_att, p.ff.rc_rep, p.ff.rc_icg, p.contact_cutoff, CCP_MIS});
+  float need = std::max({p.ff.rc_att, p.ff.rc_rep, p.ff.rc_icg, p.contact_cutoff, p.ff.mis});
   float def_cs = (p.preset == PRESET_CCP) ? CCP_ACO : need;
   p.cell_side = pm.get<float>("cell_side", std::max(def_cs, need));
   if (!(p.cell_side >= need && p.cell_side < 1.0e3f)) fail("cell_side below interaction cutoff");

@@ -172,9 +172,12 @@ __device__ __forceinline__ bool wall_vector(float3 r, const SysDesc &s, float3 &
   return isfinite(l);
 }
 
-// Wall force (chrsim.cu:79-88 for the Wang-Frenkel form).
+// Wall force (chrsim.cu:79-88 for the Wang-Frenkel form); the relaxation
+// mode always uses ccp's soft Wang-Frenkel wall.
+template <int MODE>
 __device__ __forceinline__ float wall_coef(float3 v, const ForceField &ff) {
   float d = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+  if (MODE == MODE_ICG) return (d > ICG_WALL_RC) ? 0.0f : wf_coef(1.0f, d * d);
   if (d > ff.rc_w) return 0.0f;
   float d2 = d * d;
   if (ff.pot == POT_WF) return wf_coef(ff.e_w, d2);
@@ -546,7 +549,7 @@ __global__ void __launch_bounds__(128)
 
   float3 vw;
   if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
-    float cw = wall_coef(vw, ff);
+    float cw = wall_coef<MODE>(vw, ff);
     F.x += cw * vw.x;
     F.y += cw * vw.y;
     F.z += cw * vw.z;
@@ -613,7 +616,7 @@ __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__r
   F.z += fb.z;
   float3 vw;
   if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
-    float cw = wall_coef(vw, ff);
+    float cw = wall_coef<MODE>(vw, ff);
     F.x += cw * vw.x;
     F.y += cw * vw.y;
     F.z += cw * vw.z;
@@ -629,12 +632,15 @@ __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__r
 
 // ------------------------------------------------------------------ contacts
 
-// Contact predicate shared with the oracle: |r_i - r_j| < cutoff with the
-// squared length formed as fma(dz, dz, fma(dy, dy, dx * dx)) and a correctly
-// rounded square root, so that counts are bit-exact given identical positions.
+// Contact predicate |r_i - r_j| < cutoff with the squared length rounded as
+// fma(dz, dz, fma(dx, dx, dy * dy)) and a correctly rounded square root. This
+// is the rounding of the reference's compiled length(r[x] - r[y]) < aco
+// (chrana.cu:72-73): it reproduces calc_cm on pairs within 4 ulps of the
+// cutoff, where the other orderings of the sum do not. Shared with the oracle,
+// so counts are bit-exact given identical positions.
 __device__ __forceinline__ bool in_contact(float4 a, float4 b, float cut) {
   float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
-  float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
   return __fsqrt_rn(d2) < cut;
 }
 
