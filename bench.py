@@ -1,0 +1,412 @@
+"""Benchmark of the BD engine: bead-steps/s of the batched replica ensemble.
+
+Workload: 512 independent replicas with bead counts N_i = floor(exp(U(ln 1024,
+ln 16384))) (seeded), each with its own seeded two-state Markov type sequence
+(mean block 16), 10% lamina-binding beads and Philox seed, the baseline force
+field (harmonic k=100, cosine kappa=2, WCA + A-A LJ eps=0.5 to 2.5 sigma, WCA
+wall, kT=1, dt=1e-3) in a sphere at packing fraction 0.2, and a 256x256 int32
+contact map (cutoff 1.5 sigma) per replica accumulated every 100 steps.
+Synthetic inputs; no dataset is involved.
+
+One bench step = 100 stochastic Heun steps of every replica + one contact-map /
+observable accumulation. `value` = bead-steps/s of the whole batch with the
+state resident in HBM (CUDA events on the engine's stream); `e2e` = the same
+through the C ABI with host buffers (positions uploaded from host memory and
+downloaded after every bench step). The state (~280 MB) is larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PARAMS = ("force_field baseline\ncontact_bins 256\ncontact_cutoff 1.5\n"
+          "steps_per_frame 100\npacking_fraction 0.2\n")
+HEUN_PER_STEP = 100
+B_ALG = 192.0  # algorithmic HBM bytes per bead-step of a Heun step (2 force evaluations)
+PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4 force
+METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
+
+
+def replica_sizes(n_rep, seed=2026):
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(math.log(1024), math.log(16384), n_rep))).astype(np.int32)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline
+def _walk(n, R, rng):
+    x = np.zeros((n, 3), np.float32)
+    for i in range(1, n):
+        for _ in range(100):
+            d = rng.normal(size=3)
+            p = x[i - 1] + d / np.linalg.norm(d)
+            if np.linalg.norm(p) < R - 1.0:
+                break
+        x[i] = p
+    return x
+
+
+def cpu_sample(sizes, seconds=12.0, prebuilt=None):
+    """FP32 oracle (ccp's force + Heun loop restated in C, OpenMP over all host
+    threads) on a bounded sample of replicas; returns bead-steps/s, threads, text."""
+    from oracle import oracle as orc
+
+    orc.build()
+    rng = np.random.default_rng(7)
+    ff = orc.baseline_ff()
+    systems = []
+    for k, n in enumerate(sizes):
+        R = 0.5 * (n / 0.2) ** (1 / 3)
+        if prebuilt is not None:
+            x, pt, lbs = prebuilt[k]
+        else:
+            x = _walk(int(n), R - 0.5, rng)
+            pt = np.where(rng.random(n) < 0.5, 0, 1).astype(np.int32)
+            lbs = np.zeros((0, 3), np.float32)
+        fl = orc.flags_from_types(pt, [0], "baseline")
+        geo = orc.geo_vec(R, csl=2.5)
+        if prebuilt is None:  # remove overlaps with the soft relaxation mode
+            x = orc.run(x, fl, lbs, ff, geo, 1, 0, 300, mode=orc.MODE_ICG, prec=32).astype(
+                np.float32)
+        systems.append((x, fl, lbs, geo, int(n)))
+    # calibrate the number of steps
+    t0 = time.perf_counter()
+    for x, fl, lbs, geo, n in systems:
+        orc.run(x, fl, lbs, ff, geo, 11, 0, 2, prec=32)
+    t1 = time.perf_counter()
+    per_step = max((t1 - t0) / 2, 1e-4)
+    steps = max(2, int(seconds / per_step))
+    t0 = time.perf_counter()
+    for k, (x, fl, lbs, geo, n) in enumerate(systems):
+        orc.run(x, fl, lbs, ff, geo, 100 + k, 0, steps, prec=32)
+    dt = time.perf_counter() - t0
+    beads = sum(s[4] for s in systems)
+    return beads * steps / dt, orc.lib().orc_max_threads(), \
+        "%d replicas (%d beads) x %d Heun steps, FP32" % (len(systems), beads, steps)
+
+
+def reference_arm(args, ws, rank):
+    """The reference's force/integration loop restated on the host cores (the
+    reference has no CPU implementation of its loop; its kernels are
+    __device__-only), timed on bounded samples of the same workload."""
+    if rank != 0:
+        return
+    sizes = replica_sizes(512)
+    sample = sizes[:3]
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(sample, seconds=1.0)
+    vals = []
+    descr = ""
+    cores = 1
+    for _ in range(args.steps):
+        v, cores, descr = cpu_sample(sample, seconds=3.0)
+        vals.append(v)
+    value = float(np.mean(vals))
+    beads = int(sizes.sum())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "bead-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * beads * HEUN_PER_STEP / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "c2: 512 replicas, N_i log-uniform [1024, 16384], baseline force "
+                               "field, 256^2 contact maps every 100 steps",
+                   "total_beads": beads, "heun_steps_per_step": HEUN_PER_STEP},
+        "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": cores, "kind": "port",
+                         "sample": descr},
+        "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- engine arm
+def engine_arm(args, ws, rank, local):
+    import torch
+
+    from tfm_gb300 import build as eb
+
+    eb.build()
+    from tfm_gb300.ccpgpu import Batch
+
+    torch.cuda.set_device(local)
+    sizes = replica_sizes(args.replicas)
+    seeds = np.arange(args.replicas, dtype=np.uint64) + 1 + 100000 * rank
+    b = Batch(PARAMS, sizes, seeds=seeds)
+    b.generate_initial_condition()
+    total = int(sizes.sum())
+    stream = torch.cuda.ExternalStream(b.stream())
+
+    for _ in range(args.warmup):
+        b.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    b.synchronize()
+    b.reset_observables()
+
+    clocks = Clocks(local)
+    k0 = b.kernel_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    ev1.record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = b.kernel_count() - k0
+    ms = max_over_ranks(ms, ws)
+    value = ws * total * HEUN_PER_STEP * args.steps / (ms / 1000.0)
+    ms_step = ms / args.steps
+
+    # dominant kernel (pair) timed live with CUDA events on the engine stream
+    kt = b.kernel_times(reps=5)
+    hbm, peak_kind = peaks()
+    pair_s = kt["pair"] / 1000.0
+    achieved = total * PAIR_BYTES / pair_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "pair_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                tp = json.load(f)
+            traffic = tp["bytes_per_bead"] * total
+        except Exception:
+            traffic = None
+
+    # end to end through the C ABI with host buffers
+    x = b.positions()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.set_positions(x)  # H2D through pinned staging
+        b.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+        b.synchronize()
+        x = b.positions()  # D2H of the step's result
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, ws)
+    e2e_val = ws * total * HEUN_PER_STEP * args.steps / e2e_s
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras = measure_extras(args, sizes, b)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "c2: %d replicas, N_i log-uniform [1024, 16384], baseline "
+                                   "force field, 256^2 int32 contact maps every 100 steps"
+                                   % args.replicas,
+                       "total_beads": total, "heun_steps_per_step": HEUN_PER_STEP,
+                       "l2": "state (~%d MB) larger than the 129 MB L2" % (total * 100 // 2**20),
+                       "parallelism": "replicas per GPU (no collective)"},
+            "clocks": clk,
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "pair", "achieved": achieved, "peak": hbm,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic, "bytes_per_bead": PAIR_BYTES,
+                         "pair_ms": kt["pair"]},
+            "step_roofline": {"bytes_per_bead_step": B_ALG,
+                              "achieved_gbs": value * B_ALG / 1e9,
+                              "frac": value * B_ALG / 1e9 / hbm},
+            "kernel_ms": kt,
+            "e2e": {"value": e2e_val, "unit": "bead-steps/s",
+                    "h2d_bytes_per_step": total * 16, "d2h_bytes_per_step": total * 12},
+        }
+        line.update(extras)
+        print(json.dumps(line))
+
+
+def measure_extras(args, sizes, b):
+    """Plain engine replica by replica, the large single system, the CPU baseline."""
+    import torch
+
+    from tfm_gb300.ccpgpu import Batch
+
+    out = {}
+    # plain: a sample of replicas, each alone in its own engine
+    sample = sizes[:: max(1, len(sizes) // 16)][:16]
+    tot_bs, tot_s = 0.0, 0.0
+    for k, n in enumerate(sample):
+        s = Batch(PARAMS, [int(n)], seeds=[1000 + k])
+        s.generate_initial_condition()
+        s.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+        s.synchronize()
+        st = torch.cuda.ExternalStream(s.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(3):
+            s.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+        e1.record(st)
+        s.synchronize()
+        tot_s += e0.elapsed_time(e1) / 1000.0
+        tot_bs += float(n) * HEUN_PER_STEP * 3
+        s.close()
+    plain = tot_bs / tot_s
+    out["plain_replica_by_replica"] = {"value": plain, "unit": "bead-steps/s",
+                                       "sample": "%d replicas, each alone" % len(sample)}
+    # large single system: 16 chains x 8192 beads
+    big = Batch(PARAMS.replace("contact_bins 256", "contact_bins 1024"), [131072],
+                n_chains=[16], seeds=[42])
+    big.generate_initial_condition()
+    big.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    big.synchronize()
+    st = torch.cuda.ExternalStream(big.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(5):
+        big.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    e1.record(st)
+    big.synchronize()
+    out["single_system_131072"] = {
+        "value": 131072 * HEUN_PER_STEP * 5 / (e0.elapsed_time(e1) / 1000.0),
+        "unit": "bead-steps/s", "config": "16 chains x 8192 beads, contact map 1024^2"}
+    big.close()
+    # CPU baseline: the FP32 oracle on the first replicas' initial conditions
+    pre = []
+    x = b.positions()
+    pt = b.types()
+    lbs = b.lbs()
+    for k in range(3):
+        si = b.system_info(k)
+        pre.append((x[si.bead_offset:si.bead_offset + si.n_beads],
+                    pt[si.bead_offset:si.bead_offset + si.n_beads],
+                    lbs[si.lbs_offset:si.lbs_offset + si.n_lbs]))
+    v, cores, descr = cpu_sample(sizes[:3], seconds=12.0, prebuilt=pre)
+    out["cpu_baseline"] = {"value": v, "unit": "bead-steps/s", "cores": cores, "kind": "port",
+                           "sample": descr}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, ws, rank)
+    else:
+        engine_arm(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

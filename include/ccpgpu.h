@@ -121,6 +121,26 @@ int ccpgpu_run_simulation(ccpgpu_sim *h, ccpgpu_frame_fn fn, void *user);
  * step0, step0 + observe_every, ...). */
 int ccpgpu_run_steps(ccpgpu_sim *h, uint64_t n_steps, uint32_t observe_every);
 
+/* Enqueues n_steps Heun steps on the handle's stream and returns without
+ * waiting or copying positions back (the device-resident form of
+ * ccpgpu_run_steps); ccpgpu_synchronize waits and checks the error flags.
+ * No reference counterpart (ccp's loop synchronises every frame, chrsim.cu:583). */
+int ccpgpu_advance(ccpgpu_sim *h, uint64_t n_steps, uint32_t observe_every);
+int ccpgpu_synchronize(ccpgpu_sim *h);
+
+/* The handle's cudaStream_t, for callers that time or order work against it. */
+int ccpgpu_stream_handle(ccpgpu_sim *h, void **stream);
+
+/* Average device time in ms of each kernel of one Heun step (plus one
+ * observation), measured with CUDA events around individual launches on the
+ * handle's stream over reps steps: out[0] scan (3 launches), [1] scatter,
+ * [2] pair, [3] update stage 1, [4] update stage 2, [5] contacts,
+ * [6] observe. Leaves the simulation state advanced by reps steps. */
+int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n);
+
+/* Number of engine kernels launched since creation (graph nodes included). */
+int ccpgpu_kernel_count(const ccpgpu_sim *h, uint64_t *count);
+
 /* Device error flags: [0] non-finite position, [1] bead outside its grid,
  * [2] counting-sort slot outside its system, [3] noise truncation exhausted.
  * clear != 0 resets them. Returns CCPGPU_ERR_STATE when [0] or [2] is set. */

@@ -30,7 +30,8 @@ SYMBOLS = (
     "ccpgpu_lbs_txt", "ccpgpu_frame_trr", "ccpgpu_checkpoint", "ccpgpu_load_checkpoint",
     "ccpgpu_read_frame_txt", "ccpgpu_read_lbs_txt", "ccpgpu_observe",
     "ccpgpu_reset_observables", "ccpgpu_contact_counts", "ccpgpu_observable_sums",
-    "ccpgpu_separation_counts", "ccpgpu_overlaps",
+    "ccpgpu_separation_counts", "ccpgpu_overlaps", "ccpgpu_advance", "ccpgpu_synchronize",
+    "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
 )
 
 
@@ -101,6 +102,10 @@ def load(path=LIB_PATH):
         "ccpgpu_observable_sums": [P, I32, P, SZ],
         "ccpgpu_separation_counts": [P, I32, P, P, SZ],
         "ccpgpu_overlaps": [P, P, SZ],
+        "ccpgpu_advance": [P, U64, U32], "ccpgpu_synchronize": [P],
+        "ccpgpu_stream_handle": [P, C.POINTER(P)],
+        "ccpgpu_kernel_times": [P, I32, P, SZ],
+        "ccpgpu_kernel_count": [P, C.POINTER(C.c_uint64)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -196,6 +201,30 @@ class _Handle:
 
     def run_steps(self, n, observe_every=0):
         _check(_lib.ccpgpu_run_steps(self._h, int(n), int(observe_every)))
+
+    def advance(self, n, observe_every=0):
+        """Enqueue n steps without waiting (device-resident stepping)."""
+        _check(_lib.ccpgpu_advance(self._h, int(n), int(observe_every)))
+
+    def synchronize(self):
+        _check(_lib.ccpgpu_synchronize(self._h))
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(_lib.ccpgpu_stream_handle(self._h, C.byref(s)))
+        return s.value or 0
+
+    KERNELS = ("scan", "scatter", "pair", "update1", "update2", "contacts", "observe")
+
+    def kernel_times(self, reps=5):
+        a = np.zeros(7, np.float64)
+        _check(_lib.ccpgpu_kernel_times(self._h, int(reps), _ptr(a), a.size))
+        return dict(zip(self.KERNELS, a.tolist()))
+
+    def kernel_count(self):
+        c = C.c_uint64()
+        _check(_lib.ccpgpu_kernel_count(self._h, C.byref(c)))
+        return c.value
 
     def error_flags(self, clear=False):
         a = np.zeros(8, np.int32)

@@ -90,14 +90,19 @@ struct Engine {
   DevBuf<int> d_err;
   DevBuf<float> xyz_stage;
   float *pinned[2] = {nullptr, nullptr};
+  float4 *pin_up = nullptr;  // pinned staging of position uploads
+  bool lbs_uploaded = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, int, int>, uint64_t> graph_kernels;  // kernel nodes per graph
+  uint64_t kcount = 0;  // engine kernels launched (graph nodes included)
 
   ~Engine() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
     for (int k = 0; k < 2; ++k) {
       if (pinned[k]) cudaFreeHost(pinned[k]);
+      if (k == 0 && pin_up) cudaFreeHost(pin_up);
       if (ev[k]) cudaEventDestroy(ev[k]);
     }
     if (stream) cudaStreamDestroy(stream);
@@ -228,6 +233,7 @@ struct Engine {
     d_err.alloc(ERR_COUNT);
     xyz_stage.alloc((size_t)3 * nb);
     for (int k = 0; k < 2; ++k) CK(cudaMallocHost(&pinned[k], sizeof(float) * 3 * std::max(nb, 1)));
+    CK(cudaMallocHost(&pin_up, sizeof(float4) * (nb + 1)));
 
     CK(cudaMemcpyAsync(d_sys.p, hsys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_tiles.p, htiles.data(), sizeof(Tile) * htiles.size(),
@@ -256,10 +262,11 @@ struct Engine {
     for (int c = 0; c < nch; ++c) hflags[chain_first[c]] |= BF_START;
   }
 
-  // Uploads positions + flags and rebuilds the cell histogram of pos.
+  // Uploads positions + flags (through pinned staging) and rebuilds the cell
+  // histogram of pos.
   void upload_positions() {
     set_chain_flags();
-    std::vector<float4> v(nb + 1);
+    float4 *v = pin_up;
     for (int i = 0; i < nb; ++i) {
       uint32_t w = hflags[i];
       float wf;
@@ -270,9 +277,9 @@ struct Engine {
     float wsf;
     std::memcpy(&wsf, &ws, 4);
     v[nb] = make_float4(0, 0, 0, wsf);
-    CK(cudaMemcpyAsync(pos.p, v.data(), sizeof(float4) * (nb + 1), cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemcpyAsync(pos.p, v, sizeof(float4) * (nb + 1), cudaMemcpyHostToDevice, stream));
     recount();
+    CK(cudaStreamSynchronize(stream));
     positions_valid = true;
   }
 
@@ -281,6 +288,7 @@ struct Engine {
     k_count<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, counts.p,
                                                            rank.p, d_err.p);
     CK(cudaGetLastError());
+    kcount += 1;
   }
 
   // LBS of every system sorted by cell (static during a run).
@@ -321,6 +329,7 @@ struct Engine {
     CK(cudaMemcpyAsync(lbs_start.p, st.data(), sizeof(uint32_t) * (nc + 1), cudaMemcpyHostToDevice,
                        stream));
     CK(cudaStreamSynchronize(stream));
+    lbs_uploaded = true;
   }
 
   void download_positions() {
@@ -336,17 +345,20 @@ struct Engine {
     k_scan_reduce<<<nblk, SCAN_THREADS, 0, stream>>>(counts.p, bsum.p);
     k_scan_top<<<1, SCAN_TOP_THREADS, 0, stream>>>(bsum.p, nblk, d_step.p, bump ? 1 : 0);
     k_scan_apply<<<nblk, SCAN_THREADS, 0, stream>>>(counts.p, bsum.p, start.p, nc, nblk);
+    kcount += 3;
   }
 
   void launch_scatter(const float4 *src) {
     k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, src, rank.p,
                                                              start.p, sorted.p, d_err.p);
+    kcount += 1;
   }
 
   template <int MODE>
   void launch_pair() {
     k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                 start.p, fs.p);
+    kcount += 1;
   }
 
   template <int STAGE, int MODE>
@@ -354,6 +366,7 @@ struct Engine {
     k_update<STAGE, MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(
         d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, start.p, counts.p,
         lbs_sorted.p, lbs_start.p, d_step.p, d_err.p);
+    kcount += 1;
   }
 
   ContactArgs contact_args(bool do_map, bool do_ps, bool do_ovl) {
@@ -374,11 +387,21 @@ struct Engine {
   }
 
   // Observables on the cell-ordered copy of pos (must be current).
-  void launch_observe_sorted(bool with_sdist) {
+  void launch_contacts() {
     k_contacts<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p, start.p,
                                                               contact_args(true, true, false));
+    kcount += 1;
+  }
+
+  void launch_observe() {
     k_observe<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p,
                                                              CCP_RCO / 2.0f, obs.p);
+    kcount += 1;
+  }
+
+  void launch_observe_sorted(bool with_sdist) {
+    launch_contacts();
+    launch_observe();
     if (with_sdist) {
       int smax = 0, lmax = 0;
       for (int c = 0; c < nch; ++c) {
@@ -391,6 +414,7 @@ struct Engine {
           if (chain_smax[c] == 0) continue;
           k_sdist<<<grid, 128, 0, stream>>>(pos.p, d_chain_first.p, d_chain_len.p,
                                             d_chain_ps_off.p, d_chain_smax.p, c, ds.p);
+          kcount += 1;
         }
       }
     }
@@ -415,6 +439,7 @@ struct Engine {
     auto it = graphs.find(key);
     if (it != graphs.end()) return it->second;
     cudaGraph_t g;
+    uint64_t k0 = kcount;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < n; ++k) {
       if (mode == MODE_DST)
@@ -423,6 +448,8 @@ struct Engine {
         launch_step<MODE_ICG>(false);
     }
     cudaError_t e = cudaStreamEndCapture(stream, &g);
+    graph_kernels[key] = kcount - k0;  // captured, not executed: counted per replay
+    kcount = k0;
     if (e != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e));
     cudaGraphExec_t ge;
     e = cudaGraphInstantiate(&ge, g, 0);
@@ -432,12 +459,62 @@ struct Engine {
     return ge;
   }
 
+  // Per-kernel device times of `reps` observed steps, each kernel bracketed by
+  // its own pair of events on the engine stream.
+  void kernel_times(int reps, double *out) {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    cudaEvent_t e[11];
+    for (auto &x : e) CK(cudaEventCreate(&x));
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    set_device_step();
+    for (int r = 0; r < reps; ++r) {
+      CK(cudaEventRecord(e[0], stream));
+      launch_scan(true);
+      CK(cudaEventRecord(e[1], stream));
+      launch_scatter(pos.p);
+      CK(cudaEventRecord(e[2], stream));
+      launch_contacts();
+      CK(cudaEventRecord(e[3], stream));
+      launch_observe();
+      CK(cudaEventRecord(e[4], stream));
+      launch_pair<MODE_DST>();
+      CK(cudaEventRecord(e[5], stream));
+      launch_update<1, MODE_DST>();
+      CK(cudaEventRecord(e[6], stream));
+      launch_scan(false);
+      CK(cudaEventRecord(e[7], stream));
+      launch_scatter(er.p);
+      CK(cudaEventRecord(e[8], stream));
+      launch_pair<MODE_DST>();
+      CK(cudaEventRecord(e[9], stream));
+      launch_update<2, MODE_DST>();
+      CK(cudaEventRecord(e[10], stream));
+      CK(cudaEventSynchronize(e[10]));
+      float t[10];
+      for (int k = 0; k < 10; ++k) CK(cudaEventElapsedTime(&t[k], e[k], e[k + 1]));
+      acc[0] += 0.5 * (t[0] + t[6]);
+      acc[1] += 0.5 * (t[1] + t[7]);
+      acc[2] += 0.5 * (t[4] + t[8]);
+      acc[3] += t[5];
+      acc[4] += t[9];
+      acc[5] += t[2];
+      acc[6] += t[3];
+      ++step;
+      ++dev_next;
+      ++frames_observed;
+    }
+    for (auto &x : e) cudaEventDestroy(x);
+    for (int k = 0; k < 7; ++k) out[k] = acc[k] / reps;
+    sync_and_check();
+  }
+
   // The device counter holds the step being executed; every step's first scan
   // advances it, so it only needs setting when the host moves `step`.
   void set_device_step() {
     if (dev_next == step) return;
     k_set_step<<<1, 1, 0, stream>>>(d_step.p, (unsigned long long)(step - 1));
     CK(cudaGetLastError());
+    kcount += 1;
     dev_next = step;
   }
 
@@ -463,6 +540,7 @@ struct Engine {
         g = (int)std::min<uint64_t>(left, chunk);
       }
       CK(cudaGraphLaunch(graph_for(mode, g, obs), stream));
+      kcount += graph_kernels[std::make_tuple(mode, g, obs ? 1 : 0)];
       if (obs) ++frames_observed;
       step += g;
       dev_next += g;
@@ -815,6 +893,42 @@ int ccpgpu_run_steps(ccpgpu_sim *h, uint64_t n_steps, uint32_t observe_every) {
   });
 }
 
+int ccpgpu_advance(ccpgpu_sim *h, uint64_t n_steps, uint32_t observe_every) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->run_steps(n_steps, MODE_DST, observe_every);
+  });
+}
+
+int ccpgpu_synchronize(ccpgpu_sim *h) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->sync_and_check();
+  });
+}
+
+int ccpgpu_stream_handle(ccpgpu_sim *h, void **stream) {
+  return guarded([&] {
+    need(h && stream, "null argument");
+    *stream = (void *)h->e->stream;
+  });
+}
+
+int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n) {
+  return guarded([&] {
+    need(h && out && reps > 0, "null argument");
+    need(n >= 7, "buffer too small");
+    h->e->kernel_times(reps, out);
+  });
+}
+
+int ccpgpu_kernel_count(const ccpgpu_sim *h, uint64_t *count) {
+  return guarded([&] {
+    need(h && count, "null argument");
+    *count = h->e->kcount;
+  });
+}
+
 int ccpgpu_error_flags(ccpgpu_sim *h, int32_t *flags8, int32_t clear) {
   return guarded([&] {
     need(h && flags8, "null argument");
@@ -842,7 +956,7 @@ int ccpgpu_set_positions(ccpgpu_sim *h, const float *xyz, size_t n) {
     Engine &e = *h->e;
     need(n >= (size_t)3 * e.nb, "buffer too small");
     std::memcpy(e.hxyz.data(), xyz, sizeof(float) * 3 * e.nb);
-    e.upload_lbs();
+    if (!e.lbs_uploaded) e.upload_lbs();
     e.upload_positions();
   });
 }
