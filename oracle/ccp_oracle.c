@@ -42,7 +42,7 @@
 /* force-field vector layout (double ff[FF_N]) */
 enum {
   FF_POT, FF_BEND_ALL, FF_KE, FF_L0, FF_KB, FF_EATT, FF_EREP, FF_RCREP, FF_RCATT,
-  FF_EW, FF_RCW, FF_EL, FF_LCO, FF_LBSDEPTH, FF_KICG, FF_RCICG, FF_DT, FF_SD, FF_N
+  FF_EW, FF_RCW, FF_EL, FF_LCO, FF_LBSDEPTH, FF_KICG, FF_RCICG, FF_DT, FF_SD, FF_MAXSTEP, FF_N
 };
 /* geometry vector layout (double geo[GEO_N]) */
 enum { G_RN, G_RO, G_RB, G_CSL, G_N };

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "_build", "libccporacle.so")
 F_A, F_LAD, F_HEAD = 1, 2, 4
 MODE_DST, MODE_ICG = 0, 1
 FF_KEYS = ("pot", "bend_all", "k_e", "l_0", "k_b", "e_att", "e_rep", "rc_rep", "rc_att",
-           "e_w", "rc_w", "e_l", "lco", "lbs_depth", "k_icg", "rc_icg", "dt", "sd")
+           "e_w", "rc_w", "e_l", "lco", "lbs_depth", "k_icg", "rc_icg", "dt", "sd", "max_step")
 
 RCO = 1.154701   # chrdat.cuh:20
 ACO = 2.0        # chrdat.cuh:21
@@ -38,7 +38,7 @@ def ccp_ff(T=298.0):
     return dict(pot=0, bend_all=0, k_e=128.0, l_0=1.0, k_b=1.0, e_att=0.5, e_rep=0.5,
                 rc_rep=f32(RCO), rc_att=ACO, e_w=1.0, rc_w=f32(RCO), e_l=8.0, lco=LCO,
                 lbs_depth=f32(RCO), k_icg=128.0, rc_icg=f32(RCO), dt=f32(dt),
-                sd=f32(math.sqrt(2.0 * float(np.float32(K_B)) * float(np.float32(T)) * dt)))
+                sd=f32(math.sqrt(2.0 * float(np.float32(K_B)) * float(np.float32(T)) * dt)), max_step=0.0)
 
 
 def baseline_ff(kT=1.0, dt=1e-3):
@@ -47,7 +47,7 @@ def baseline_ff(kT=1.0, dt=1e-3):
     return dict(pot=1, bend_all=1, k_e=100.0, l_0=1.0, k_b=2.0, e_att=0.5, e_rep=1.0,
                 rc_rep=wca, rc_att=2.5, e_w=1.0, rc_w=wca, e_l=8.0, lco=LCO, lbs_depth=wca,
                 k_icg=128.0, rc_icg=f32(RCO), dt=f32(dt),
-                sd=f32(math.sqrt(2.0 * f32(kT) * f32(dt))))
+                sd=f32(math.sqrt(2.0 * f32(kT) * f32(dt))), max_step=0.1)
 
 
 def ff_vec(ff):

@@ -16,9 +16,20 @@ static inline REAL SFX(dot)(SFX(v3) a, SFX(v3) b) { return a.x * b.x + a.y * b.y
 typedef struct {
   int pot, bend_all;
   REAL k_e, l_0, k_b, e_att, e_rep, rc_rep, rc_att, e_w, rc_w, e_l, lco, lbs_depth, k_icg,
-      rc_icg, dt, sd;
+      rc_icg, dt, sd, max_step;
   REAL R_n, R_o, R_b, noc, boc, nod, bod, d_m, csl;
 } SFX(model);
+
+/* Deterministic displacement of one stage limited to max_step (> 0); the
+ * baseline preset's stabiliser of the WCA core at dt = 1e-3 (not in ccp). */
+static inline void SFX(cap_step)(REAL *dx, REAL *dy, REAL *dz, REAL max_step) {
+  if (max_step <= 0) return;
+  REAL m2 = *dx * *dx + *dy * *dy + *dz * *dz;
+  if (m2 > max_step * max_step) {
+    REAL k = max_step / SQRT(m2);
+    *dx *= k; *dy *= k; *dz *= k;
+  }
+}
 
 static SFX(model) SFX(make_model)(const double *ff, const double *geo) {
   SFX(model) m;
@@ -40,6 +51,7 @@ static SFX(model) SFX(make_model)(const double *ff, const double *geo) {
   m.rc_icg = (REAL)ff[FF_RCICG];
   m.dt = (REAL)ff[FF_DT];
   m.sd = (REAL)ff[FF_SD];
+  m.max_step = (REAL)ff[FF_MAXSTEP];
   /* cngeom (chrdat.cu:13-18) */
   double R_n = geo[G_RN], R_o = geo[G_RO], R_b = geo[G_RB];
   double noc = cos(asin(R_o / R_n)), boc = cos(asin(R_o / R_b));
@@ -402,17 +414,21 @@ void SFX(orc_run)(int n, const float *xyz, const uint32_t *flags, int n_l, const
     SFX(forces_core)(n, r, flags, n_l, l, &m, mode, 1, head, end, f1, NULL);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
-      er[i].x = r[i].x + f1[i].x * m.dt + rn[i].x;
-      er[i].y = r[i].y + f1[i].y * m.dt + rn[i].y;
-      er[i].z = r[i].z + f1[i].z * m.dt + rn[i].z;
+      REAL dx = f1[i].x * m.dt, dy = f1[i].y * m.dt, dz = f1[i].z * m.dt;
+      SFX(cap_step)(&dx, &dy, &dz, m.max_step);
+      er[i].x = r[i].x + dx + rn[i].x;
+      er[i].y = r[i].y + dy + rn[i].y;
+      er[i].z = r[i].z + dz + rn[i].z;
     }
     SFX(forces_core)(n, er, flags, n_l, l, &m, mode, 1, head, end, f2, NULL);
     REAL h = (REAL)0.5 * m.dt;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
-      r[i].x = r[i].x + (f1[i].x + f2[i].x) * h + rn[i].x;
-      r[i].y = r[i].y + (f1[i].y + f2[i].y) * h + rn[i].y;
-      r[i].z = r[i].z + (f1[i].z + f2[i].z) * h + rn[i].z;
+      REAL dx = (f1[i].x + f2[i].x) * h, dy = (f1[i].y + f2[i].y) * h, dz = (f1[i].z + f2[i].z) * h;
+      SFX(cap_step)(&dx, &dy, &dz, m.max_step);
+      r[i].x = r[i].x + dx + rn[i].x;
+      r[i].y = r[i].y + dy + rn[i].y;
+      r[i].z = r[i].z + dz + rn[i].z;
     }
   }
   for (int i = 0; i < n; ++i) {

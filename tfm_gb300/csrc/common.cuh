@@ -55,6 +55,7 @@ struct ForceField {
   float k_icg;      // soft repulsion of the ICG mode (128)
   float rc_icg;     // soft repulsion cutoff (rco)
   float mis;        // relaxation ends when no non-bonded pair is closer (chrsim.cuh:20)
+  float max_step;   // cap on the deterministic displacement of one stage (0: none)
   float dt;         // time step
   float sd;         // noise standard deviation sqrt(2 kT dt)
   float kT;         // thermal energy
@@ -70,6 +71,7 @@ struct SysDesc {
   float R_n, R_o, R_b;       // nucleus, opening and bleb radii
   float noc, boc, nod, bod;  // derived geometry (chrdat.cu:13-18)
   int32_t lbs_off, n_lbs;    // LBS, sorted by cell, [lbs_off, lbs_off + n_lbs)
+  float lbs_rmin, lbs_rmax;  // radial extent of the system's LBS
   uint32_t seed_lo, seed_hi; // Philox key
   int32_t chain_off, n_chains;
   // contact map (packed lower triangle of nbins x nbins int32 counts)

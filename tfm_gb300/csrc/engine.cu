@@ -148,6 +148,8 @@ struct Engine {
       d.bod = g.bod;
       d.lbs_off = nl;
       d.n_lbs = q.n_lbs;
+      d.lbs_rmin = 1e30f;  // set from the sites by upload_lbs
+      d.lbs_rmax = -1e30f;
       d.seed_lo = (uint32_t)q.seed;
       d.seed_hi = (uint32_t)(q.seed >> 32);
       d.chain_off = nch;
@@ -296,9 +298,15 @@ struct Engine {
     std::vector<uint32_t> cnt(nc + 1, 0);
     std::vector<int> cell_of_l(nl);
     for (size_t s = 0; s < hsys.size(); ++s) {
-      const SysDesc &d = hsys[s];
+      SysDesc &d = hsys[s];
+      d.lbs_rmin = 1e30f;
+      d.lbs_rmax = -1e30f;
       for (int k = 0; k < d.n_lbs; ++k) {
         int l = d.lbs_off + k;
+        float r = std::sqrt(hlbs[3 * l] * hlbs[3 * l] + hlbs[3 * l + 1] * hlbs[3 * l + 1] +
+                            hlbs[3 * l + 2] * hlbs[3 * l + 2]);
+        d.lbs_rmin = std::min(d.lbs_rmin, r * 0.9999f - 1e-4f);
+        d.lbs_rmax = std::max(d.lbs_rmax, r * 1.0001f + 1e-4f);
         int c[3];
         for (int a = 0; a < 3; ++a) {
           float v = hlbs[3 * l + a];
@@ -327,6 +335,8 @@ struct Engine {
     CK(cudaMemcpyAsync(lbs_sorted.p, srt.data(), sizeof(float4) * std::max(nl, 1),
                        cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(lbs_start.p, st.data(), sizeof(uint32_t) * (nc + 1), cudaMemcpyHostToDevice,
+                       stream));
+    CK(cudaMemcpyAsync(d_sys.p, hsys.data(), sizeof(SysDesc) * hsys.size(), cudaMemcpyHostToDevice,
                        stream));
     CK(cudaStreamSynchronize(stream));
     lbs_uploaded = true;

@@ -84,6 +84,7 @@ static ForceField preset_ccp(float T) {
   f.k_icg = 128.0f;
   f.rc_icg = CCP_RCO;
   f.mis = CCP_MIS;
+  f.max_step = 0.0f;
   f.dt = (float)CCP_DT;
   f.kT = CCP_K_B * T;
   f.sd = (float)std::sqrt(2.0 * CCP_K_B * T * CCP_DT);  // chrsim.cu:424
@@ -111,6 +112,9 @@ static ForceField preset_baseline(float kT, float dt) {
   f.rc_icg = CCP_RCO;
   // WCA with dt = 1e-3 is stable (dt |dF/dr| < 2) only beyond r ~ 0.92
   f.mis = 0.95f;
+  // a 5-sigma noise jump can bring a WCA pair to r ~ 0.7, where one corrector
+  // step would move it several sigma: cap the deterministic displacement
+  f.max_step = 0.1f;
   f.dt = dt;
   f.kT = kT;
   f.sd = (float)std::sqrt(2.0 * (double)kT * (double)dt);

@@ -415,9 +415,8 @@ __device__ __forceinline__ float3 lbs_force(float4 x, const SysDesc &s, const Fo
                                             const uint32_t *__restrict__ lbs_start) {
   float3 f = make_float3(0.0f, 0.0f, 0.0f);
   float d = sqrtf(x.x * x.x + x.y * x.y + x.z * x.z);
-  float rl = s.R_n - ff.lbs_depth;
-  if (fabsf(d - rl) > ff.lco * 1.001f + 1e-3f) return f;
   float m = ff.lco * 1.001f + 1e-4f;
+  if (d < s.lbs_rmin - m || d > s.lbs_rmax + m) return f;  // no site within reach
   bool esc = false;
   int xl = cell_coord(x.x - m, s.inv_csl, s.cps, esc), xh = cell_coord(x.x + m, s.inv_csl, s.cps, esc);
   int yl = cell_coord(x.y - m, s.inv_csl, s.cps, esc), yh = cell_coord(x.y + m, s.inv_csl, s.cps, esc);
@@ -509,6 +508,20 @@ __device__ __forceinline__ float3 bonded_force(const float4 *__restrict__ X, int
   return f;
 }
 
+// Deterministic displacement of one stage limited to max_step (> 0): keeps the
+// stiff WCA core stable at dt = 1e-3 when a truncated-noise jump brings a pair
+// deep into it; inactive for |F| dt <= max_step. ccp's preset sets no cap.
+__device__ __forceinline__ void cap_step(float3 &D, float max_step) {
+  if (max_step <= 0.0f) return;
+  float m2 = D.x * D.x + D.y * D.y + D.z * D.z;
+  if (m2 > max_step * max_step) {
+    float k = max_step * rsqrtf(m2);
+    D.x *= k;
+    D.y *= k;
+    D.z *= k;
+  }
+}
+
 // Fused chain-order pass of one Heun stage.
 //   STAGE 1: X = r.  f = F(r);  er = r + f dt + sd z           (chrsim.cu:365-388)
 //   STAGE 2: X = er. ef = F(er); r = r + (f + ef) dt / 2 + sd z (chrsim.cu:392-416)
@@ -569,16 +582,18 @@ __global__ void __launch_bounds__(128)
 
   float4 out;
   if (STAGE == 1) {
-    out = make_float4(xi.x + F.x * ff.dt + rn.x, xi.y + F.y * ff.dt + rn.y,
-                      xi.z + F.z * ff.dt + rn.z, xi.w);
+    float3 D = make_float3(F.x * ff.dt, F.y * ff.dt, F.z * ff.dt);
+    cap_step(D, ff.max_step);
+    out = make_float4(xi.x + D.x + rn.x, xi.y + D.y + rn.y, xi.z + D.z + rn.z, xi.w);
     er[i] = out;
     fbuf[i] = make_float4(F.x, F.y, F.z, 0.0f);
   } else {
     float4 r = pos[i];
     float4 f1 = fbuf[i];
     float h = 0.5f * ff.dt;
-    out = make_float4(r.x + (f1.x + F.x) * h + rn.x, r.y + (f1.y + F.y) * h + rn.y,
-                      r.z + (f1.z + F.z) * h + rn.z, r.w);
+    float3 D = make_float3((f1.x + F.x) * h, (f1.y + F.y) * h, (f1.z + F.z) * h);
+    cap_step(D, ff.max_step);
+    out = make_float4(r.x + D.x + rn.x, r.y + D.y + rn.y, r.z + D.z + rn.z, r.w);
     pos[i] = out;
   }
   if (!(isfinite(out.x) && isfinite(out.y) && isfinite(out.z))) set_err(err, ERR_NAN);
