@@ -92,6 +92,21 @@ def test_forces_baseline_match_fp64_oracle(base_sim, orc, steps):
     assert err <= FORCE_RTOL
 
 
+def test_pair_kernels_agree(ccp_sim, orc):
+    """The thread-per-bead and the warp-per-cell pair kernels give the same forces."""
+    from tfm_gb300.ccpgpu import ChrSim
+
+    sim, R = ccp_sim
+    txt, _, _ = ccp_params(2048, laf=0.3)
+    other = ChrSim(txt + "pair_kernel 0\n", seed=7)
+    other.set_types(sim.types())
+    other.set_lbs(sim.lbs())
+    other.set_positions(sim.positions())
+    (f64, sa), fl, geo = _oracle_forces(orc, sim, orc.ccp_ff(), 2.0, [0])
+    assert _force_ok(other.forces(), f64, sa) <= FORCE_RTOL
+    assert _force_ok(sim.forces(), f64, sa) <= FORCE_RTOL
+
+
 def _golden_cases():
     return sorted(glob.glob(os.path.join(GOLDEN, "ccp_*.npz")))
 

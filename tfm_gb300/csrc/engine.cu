@@ -59,7 +59,8 @@ struct Engine {
   std::vector<SystemSpec> specs;
   std::vector<SysDesc> hsys;
   std::vector<Geometry> geo;
-  std::vector<Tile> htiles;
+  std::vector<Tile> htiles;   // bead tiles (chain order / cell order)
+  std::vector<Tile> hctiles;  // cell tiles: PAIR_WARPS cells of one x-row
   int nb = 0, nc = 0, nl = 0, nch = 0;
   int nblk = 0;        // scan CTAs
   int64_t map_total = 0;
@@ -80,7 +81,7 @@ struct Engine {
 
   // device state
   DevBuf<SysDesc> d_sys;
-  DevBuf<Tile> d_tiles;
+  DevBuf<Tile> d_tiles, d_ctiles;
   DevBuf<float4> pos, er, fbuf, fs, sorted, lbs_sorted, fout;
   DevBuf<uint32_t> rank, counts, start, bsum, lbs_start;
   DevBuf<int32_t> d_chain_of, d_chain_first, d_chain_len, d_chain_ps_off, d_chain_smax;
@@ -197,6 +198,13 @@ struct Engine {
     htiles.clear();
     for (int s = 0; s < ns; ++s)
       for (int b = 0; b < hsys[s].n; b += TILE) htiles.push_back(Tile{s, hsys[s].bead_off + b});
+    hctiles.clear();
+    for (int s = 0; s < ns; ++s) {
+      const int cps = hsys[s].cps;
+      for (int row = 0; row < cps * cps; ++row)
+        for (int x = 0; x < cps; x += PAIR_WARPS)
+          hctiles.push_back(Tile{s, hsys[s].cell_off + row * cps + x});
+    }
     nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
 
     hxyz.assign((size_t)3 * nb, 0.0f);
@@ -208,6 +216,7 @@ struct Engine {
     for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
     d_sys.alloc(ns);
     d_tiles.alloc(htiles.size());
+    d_ctiles.alloc(hctiles.size());
     pos.alloc(nb + 1);
     er.alloc(nb + 1);
     fbuf.alloc(nb + 1);
@@ -239,6 +248,8 @@ struct Engine {
 
     CK(cudaMemcpyAsync(d_sys.p, hsys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_tiles.p, htiles.data(), sizeof(Tile) * htiles.size(),
+                       cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_ctiles.p, hctiles.data(), sizeof(Tile) * hctiles.size(),
                        cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_chain_of.p, chain_of.data(), 4 * nb, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_chain_first.p, chain_first.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
@@ -366,8 +377,12 @@ struct Engine {
 
   template <int MODE>
   void launch_pair() {
-    k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
-                                                                start.p, fs.p);
+    if (par.pair_kernel == 0)
+      k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                                  start.p, fs.p);
+    else
+      k_pair_cells<MODE><<<(unsigned)hctiles.size(), PAIR_WARPS * 32, 0, stream>>>(
+          d_ctiles.p, d_sys.p, ff, sorted.p, start.p, fs.p);
     kcount += 1;
   }
 

@@ -137,51 +137,105 @@ __device__ __forceinline__ float pair_coef(float d2, bool hh, const ForceField &
   return lj_coef(hh ? ff.e_att : ff.e_rep, d2);
 }
 
-// Wall-particle vector of ccp's nucleus + opening + bleb geometry
-// (chrsim.cu:92-137); the ICG mode uses the bare sphere (chrsim.cu:148-163).
-// Returns false when the vector is not finite (no wall force, chrsim.cu:137).
-template <int MODE>
-__device__ __forceinline__ bool wall_vector(float3 r, const SysDesc &s, float3 &v) {
-  if (MODE == MODE_ICG) {
-    float d = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
-    float k = -r_over_d_minus1(s.R_n, r.x, r.y, r.z, d);
-    v = make_float3(r.x * k, r.y * k, r.z * k);
-  } else if (r.z < s.nod) {
-    float d = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
-    if (r.z / d < s.noc) {
-      float k = -r_over_d_minus1(s.R_n, r.x, r.y, r.z, d);
-      v = make_float3(r.x * k, r.y * k, r.z * k);
-    } else {
-      d = sqrtf(r.x * r.x + r.y * r.y);
-      float k = -r_over_d_minus1(s.R_o, r.x, r.y, 0.0f, d);
-      v = make_float3(r.x * k, r.y * k, r.z - s.nod);
-    }
-  } else {
-    float3 q = make_float3(r.x, r.y, r.z - (s.nod + s.bod));
-    float d = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
-    if (-q.z / d < s.boc) {
-      float k = -r_over_d_minus1(s.R_b, q.x, q.y, q.z, d);
-      v = make_float3(q.x * k, q.y * k, q.z * k);
-    } else {
-      d = sqrtf(q.x * q.x + q.y * q.y);
-      float k = -r_over_d_minus1(s.R_o, q.x, q.y, 0.0f, d);
-      v = make_float3(q.x * k, q.y * k, q.z + s.bod);
-    }
-  }
-  float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-  return isfinite(l);
+// Distance d of (a, b, c) from the origin and the gap g = R - d carried as a
+// double-float gh + gl (pairs of FP32 words), from R^2 - d^2 formed without
+// cancellation. The wall potentials depend on g^2 near their cutoffs, where a
+// single-float g (rounding 6e-8) would leave ~1e-5 relative force error.
+__device__ __forceinline__ void gap_df(float R, float a, float b, float c, float &dist,
+                                       float &gh, float &gl) {
+  float pa = __fmul_rn(a, a), ea = __fmaf_rn(a, a, -pa);
+  float pb = __fmul_rn(b, b), eb = __fmaf_rn(b, b, -pb);
+  float pc = __fmul_rn(c, c), ec = __fmaf_rn(c, c, -pc);
+  float s1 = __fadd_rn(pa, pb), e1 = two_sum_err(pa, pb, s1);
+  float s2 = __fadd_rn(s1, pc), e2 = two_sum_err(s1, pc, s2);
+  float lo = __fadd_rn(__fadd_rn(ea, eb), __fadd_rn(ec, __fadd_rn(e1, e2)));
+  float d2h = __fadd_rn(s2, lo), d2l = __fsub_rn(lo, __fsub_rn(d2h, s2));
+  float dh = sqrtf(d2h);
+  float dl = (dh > 0.0f) ? __fadd_rn(__fmaf_rn(-dh, dh, d2h), d2l) / (2.0f * dh) : 0.0f;
+  float rh = __fmul_rn(R, R), rl = __fmaf_rn(R, R, -rh);
+  float nh = __fsub_rn(rh, d2h);
+  float nl = __fadd_rn(two_sum_err(rh, -d2h, nh), __fsub_rn(rl, d2l));
+  float deh = __fadd_rn(R, dh);
+  float del = __fadd_rn(two_sum_err(R, dh, deh), dl);
+  float qh = nh / deh;
+  float rr = __fsub_rn(__fadd_rn(__fmaf_rn(-qh, deh, nh), nl), __fmul_rn(qh, del));
+  float ql = rr / deh;
+  gh = __fadd_rn(qh, ql);
+  gl = __fsub_rn(ql, __fsub_rn(gh, qh));
+  dist = dh;
 }
 
-// Wall force (chrsim.cu:79-88 for the Wang-Frenkel form); the relaxation
-// mode always uses ccp's soft Wang-Frenkel wall.
+// Wall-particle vector v of ccp's nucleus + opening + bleb geometry
+// (chrsim.cu:92-137; the ICG mode uses the bare sphere, chrsim.cu:148-163),
+// with |v| = gh + gl. Returns false when v is not finite (no wall force,
+// chrsim.cu:137).
 template <int MODE>
-__device__ __forceinline__ float wall_coef(float3 v, const ForceField &ff) {
-  float d = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-  if (MODE == MODE_ICG) return (d > ICG_WALL_RC) ? 0.0f : wf_coef(1.0f, d * d);
-  if (d > ff.rc_w) return 0.0f;
-  float d2 = d * d;
-  if (ff.pot == POT_WF) return wf_coef(ff.e_w, d2);
-  return lj_coef(ff.e_w, d2);
+__device__ __forceinline__ bool wall_vector(float3 r, const SysDesc &s, float3 &v, float &gh,
+                                            float &gl) {
+  float3 q = r;
+  float R = s.R_n;
+  bool sphere = true;
+  if (MODE != MODE_ICG) {
+    if (r.z < s.nod) {
+      float d = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+      if (!(r.z / d < s.noc)) {
+        d = sqrtf(r.x * r.x + r.y * r.y);
+        float k = -r_over_d_minus1(s.R_o, r.x, r.y, 0.0f, d);
+        v = make_float3(r.x * k, r.y * k, r.z - s.nod);
+        sphere = false;
+      }
+    } else {
+      q = make_float3(r.x, r.y, r.z - (s.nod + s.bod));
+      R = s.R_b;
+      float d = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
+      if (!(-q.z / d < s.boc)) {
+        d = sqrtf(q.x * q.x + q.y * q.y);
+        float k = -r_over_d_minus1(s.R_o, q.x, q.y, 0.0f, d);
+        v = make_float3(q.x * k, q.y * k, q.z + s.bod);
+        sphere = false;
+      }
+    }
+  }
+  if (sphere) {
+    float d;
+    gap_df(R, q.x, q.y, q.z, d, gh, gl);
+    float k = -gh / d;  // -(R/d - 1)
+    v = make_float3(q.x * k, q.y * k, q.z * k);
+    if (gh < 0.0f) {  // outside: |v| = d - R
+      gh = -gh;
+      gl = -gl;
+    }
+  } else {
+    gh = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    gl = 0.0f;
+  }
+  float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+  return isfinite(l) && isfinite(gh);
+}
+
+// Wall force coefficient c (F = c v) from the double-float distance g = gh + gl
+// (chrsim.cu:79-88 for the Wang-Frenkel form); the relaxation mode always uses
+// ccp's soft Wang-Frenkel wall. Both forms are evaluated from g^2 without the
+// cancellation at their cutoffs: WF 6e (g^2 - 4)(3 g^2 - 4) / g^8 and
+// LJ 24e (2 - g^6) / g^14.
+template <int MODE>
+__device__ __forceinline__ float wall_coef(float gh, float gl, const ForceField &ff) {
+  const bool wf = (MODE == MODE_ICG) || (ff.pot == POT_WF);
+  const float e = (MODE == MODE_ICG) ? 1.0f : ff.e_w;
+  if (gh > ((MODE == MODE_ICG) ? ICG_WALL_RC : ff.rc_w)) return 0.0f;
+  float h2h = __fmul_rn(gh, gh);
+  float h2l = __fadd_rn(__fmaf_rn(gh, gh, -h2h), 2.0f * gh * gl);
+  float i2 = 1.0f / h2h, i4 = i2 * i2;
+  if (wf) {
+    float a = __fadd_rn(__fsub_rn(h2h, 4.0f), h2l);
+    float b = __fadd_rn(__fmaf_rn(3.0f, h2h, -4.0f), 3.0f * h2l);
+    return 6.0f * e * (a * b) * (i4 * i4);
+  }
+  float p1 = __fmul_rn(h2h, h2h), e1 = __fmaf_rn(h2h, h2h, -p1);
+  float p2 = __fmul_rn(p1, h2h), e2 = __fmaf_rn(p1, h2h, -p2);
+  float lo6 = __fadd_rn(__fadd_rn(e2, e1 * h2h), 3.0f * h2h * h2h * h2l);
+  float m = __fsub_rn(__fsub_rn(2.0f, p2), lo6);
+  return 24.0f * e * m * (i4 * i2 * i2 * i2);
 }
 
 // Truncated standard normals for one bead and step: three Box-Muller normals
@@ -406,6 +460,100 @@ __global__ void __launch_bounds__(128)
   fs[slot] = make_float4(fx, fy, fz, 0.0f);
 }
 
+// Cell-major pair kernel. One warp per cell; the warp's 4 groups of 8 lanes
+// each own up to 2 of the cell's beads per pass, and the 8 lanes of a group
+// sweep the cell's 27-cell neighbourhood (9 x-contiguous ranges of the sorted
+// array, flattened) together. A warp load therefore reads 8 consecutive
+// candidates shared by all groups (one 128-byte line), trip counts are uniform
+// across the warp, and each candidate feeds two interactions. The group's
+// partial forces are combined with 3 shuffle steps. CTA = PAIR_WARPS warps =
+// up to PAIR_WARPS consecutive cells of one x-row of one system (tile table).
+constexpr int PAIR_WARPS = 8;
+constexpr int PAIR_GROUP = 8;                   // lanes per group
+constexpr int PAIR_NGROUPS = 32 / PAIR_GROUP;   // groups per warp
+constexpr int PAIR_HOME = 2 * PAIR_NGROUPS;     // home beads per warp pass
+
+template <int MODE>
+__device__ __forceinline__ void pair_accum(float4 p, uint32_t wi, float4 q, const ForceField &ff,
+                                           float3 &acc) {
+  uint32_t wj = wbits(q);
+  int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
+  if ((unsigned)(gi - gj + 1) <= 2u) return;  // |i - j| <= 1, self included
+  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  bool hh = (wi & wj & BF_HET) != 0u;
+  float cf = pair_coef<MODE>(d2, hh, ff);
+  acc.x += cf * dx;
+  acc.y += cf * dy;
+  acc.z += cf * dz;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(PAIR_WARPS * 32)
+    k_pair_cells(const Tile *__restrict__ ctiles, const SysDesc *__restrict__ sys, ForceField ff,
+                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+                 float4 *__restrict__ fs) {
+  Tile t = ctiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  const int cps = s.cps;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if ((t.begin - s.cell_off) % cps + warp >= cps) return;  // beyond the row segment
+  const int c = t.begin + warp;                              // global cell index
+  const int lc = c - s.cell_off;
+  const int cx = lc % cps, cyz = lc / cps;
+  const int cy = cyz % cps, cz = cyz / cps;
+  const uint32_t hb = start[c], he = start[c + 1];
+  if (hb == he) return;
+  // the 9 candidate ranges (x-adjacent cells of each (dy, dz) row)
+  uint32_t rb[9], rlen[9];
+  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, cps - 1);
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    int y = cy + (r % 3) - 1, z = cz + (r / 3) - 1;
+    uint32_t b = 0, e = 0;
+    if (y >= 0 && y < cps && z >= 0 && z < cps) {
+      int row = s.cell_off + (z * cps + y) * cps;
+      b = start[row + x0];
+      e = start[row + x1 + 1];
+    }
+    rb[r] = b;
+    rlen[r] = e - b;
+  }
+  const int g = lane / PAIR_GROUP, gl = lane % PAIR_GROUP;
+  for (uint32_t h0 = hb; h0 < he; h0 += PAIR_HOME) {
+    const uint32_t ha = h0 + g, hc = h0 + g + PAIR_NGROUPS;
+    const bool va = ha < he, vc = hc < he;
+    float4 pa = sorted[va ? ha : hb], pc = sorted[vc ? hc : hb];
+    uint32_t wa = wbits(pa), wc = wbits(pc);
+    float3 aa = make_float3(0.0f, 0.0f, 0.0f), ac = make_float3(0.0f, 0.0f, 0.0f);
+    // lane gl visits flattened candidates gl, gl + 8, ...: the offset carried
+    // into the next range is where the lane's stride overshot the current one
+    uint32_t k = gl;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+      for (; k < rlen[r]; k += PAIR_GROUP) {
+        float4 q = __ldg(&sorted[rb[r] + k]);
+        if (va) pair_accum<MODE>(pa, wa, q, ff, aa);
+        if (vc) pair_accum<MODE>(pc, wc, q, ff, ac);
+      }
+      k -= rlen[r];
+    }
+#pragma unroll
+    for (int o = PAIR_GROUP / 2; o > 0; o >>= 1) {
+      aa.x += __shfl_xor_sync(0xffffffffu, aa.x, o);
+      aa.y += __shfl_xor_sync(0xffffffffu, aa.y, o);
+      aa.z += __shfl_xor_sync(0xffffffffu, aa.z, o);
+      ac.x += __shfl_xor_sync(0xffffffffu, ac.x, o);
+      ac.y += __shfl_xor_sync(0xffffffffu, ac.y, o);
+      ac.z += __shfl_xor_sync(0xffffffffu, ac.z, o);
+    }
+    if (gl == 0) {
+      if (va) fs[ha] = make_float4(aa.x, aa.y, aa.z, 0.0f);
+      if (vc) fs[hc] = make_float4(ac.x, ac.y, ac.z, 0.0f);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ update
 
 // Lamina-binding force on a LAD bead at x (chrsim.cu:202-212, 261-273): sites
@@ -561,8 +709,9 @@ __global__ void __launch_bounds__(128)
   F.z += fb.z;
 
   float3 vw;
-  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
-    float cw = wall_coef<MODE>(vw, ff);
+  float gh, gl;
+  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw, gh, gl)) {
+    float cw = wall_coef<MODE>(gh, gl, ff);
     F.x += cw * vw.x;
     F.y += cw * vw.y;
     F.z += cw * vw.z;
@@ -630,8 +779,9 @@ __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__r
   F.y += fb.y;
   F.z += fb.z;
   float3 vw;
-  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw)) {
-    float cw = wall_coef<MODE>(vw, ff);
+  float gh, gl;
+  if (wall_vector<MODE>(make_float3(xi.x, xi.y, xi.z), s, vw, gh, gl)) {
+    float cw = wall_coef<MODE>(gh, gl, ff);
     F.x += cw * vw.x;
     F.y += cw * vw.y;
     F.z += cw * vw.z;
