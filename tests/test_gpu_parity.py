@@ -98,7 +98,7 @@ def test_pair_kernels_agree(ccp_sim, orc):
 
     sim, R = ccp_sim
     txt, _, _ = ccp_params(2048, laf=0.3)
-    other = ChrSim(txt + "pair_kernel 0\n", seed=7)
+    other = ChrSim(txt + "pair_kernel 1\n", seed=7)
     other.set_types(sim.types())
     other.set_lbs(sim.lbs())
     other.set_positions(sim.positions())

@@ -71,7 +71,7 @@ struct Params {
   float packing_fraction = 0.2f;
   float lbs_area_fraction = 0.25f;
   bool relaxed = false;
-  int pair_kernel = 1;  // 0: thread per bead; 1: warp per cell (lane groups)
+  int pair_kernel = 0;  // 0: thread per bead; 1: warp per cell (lane groups)
   std::string sequence_file = "Program/data/sequence.txt";
   ForceField ff{};
 };

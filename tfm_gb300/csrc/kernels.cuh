@@ -235,7 +235,8 @@ __device__ __forceinline__ float wall_coef(float gh, float gl, const ForceField 
   float p2 = __fmul_rn(p1, h2h), e2 = __fmaf_rn(p1, h2h, -p2);
   float lo6 = __fadd_rn(__fadd_rn(e2, e1 * h2h), 3.0f * h2h * h2h * h2l);
   float m = __fsub_rn(__fsub_rn(2.0f, p2), lo6);
-  return 24.0f * e * m * (i4 * i2 * i2 * i2);
+  float i6 = i4 * i2;
+  return 24.0f * e * m * (i6 * i6 * i2);  // 1 / g^14
 }
 
 // Truncated standard normals for one bead and step: three Box-Muller normals
@@ -416,6 +417,44 @@ __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restr
 
 // ------------------------------------------------------------------ pair
 
+// Branch-free pair term of the pair kernels: the coefficient is
+// evaluated for every candidate and selected to zero beyond the cutoff or for
+// |i - j| <= 1 (self included), so the lanes of a warp never diverge. The
+// reciprocal is the hardware approximation (<= 2 ulp), well inside the FP32
+// force tolerance.
+template <int MODE>
+__device__ __forceinline__ void pair_accum(float4 p, uint32_t wi, float4 q, const ForceField &ff,
+                                           float3 &acc) {
+  uint32_t wj = wbits(q);
+  int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
+  bool excl = (unsigned)(gi - gj + 1) <= 2u;
+  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  float cf;
+  if (MODE == MODE_ICG) {
+    float d = sqrtf(d2);
+    cf = ff.k_icg * (3.0f * ff.rc_icg - 3.0f * d);
+    cf = (excl || d2 > ff.rc_icg * ff.rc_icg) ? 0.0f : cf;
+  } else {
+    bool hh = (wi & wj & BF_HET) != 0u;
+    float rc = hh ? ff.rc_att : ff.rc_rep;
+    float i2 = __fdividef(1.0f, d2);
+    if (ff.pot == POT_WF) {
+      float i4 = i2 * i2;
+      cf = 6.0f * ff.e_att * (__fsub_rn(d2, 4.0f) * __fmaf_rn(3.0f, d2, -4.0f)) * (i4 * i4);
+    } else {
+      float e = hh ? ff.e_att : ff.e_rep;
+      float i6 = i2 * i2 * i2;
+      cf = 24.0f * e * (i6 * i2) * __fmaf_rn(2.0f, i6, -1.0f);
+    }
+    cf = (excl || d2 > rc * rc) ? 0.0f : cf;
+  }
+  acc.x += cf * dx;
+  acc.y += cf * dy;
+  acc.z += cf * dz;
+}
+
+
 // Excluded-volume and A-A attraction forces in cell order. Each thread owns
 // one sorted bead; for every (dy, dz) row of the 3x3x3 neighbourhood the three
 // x-adjacent cells form one contiguous range of the sorted array. Pairs with
@@ -431,13 +470,11 @@ __global__ void __launch_bounds__(128)
   if (slot >= s.bead_off + s.n) return;
   float4 p = sorted[slot];
   uint32_t wi = wbits(p);
-  int gi = (int)(wi >> BF_BITS);
-  bool het = (wi & BF_HET) != 0u;
   bool esc = false;
   CellXYZ c = cell_of(p, s, esc);
   const int cps = s.cps;
   int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
-  float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
   for (int z = max(c.z - 1, 0); z <= min(c.z + 1, cps - 1); ++z) {
     for (int y = max(c.y - 1, 0); y <= min(c.y + 1, cps - 1); ++y) {
       int row = s.cell_off + (z * cps + y) * cps;
@@ -445,19 +482,11 @@ __global__ void __launch_bounds__(128)
       uint32_t e = __ldg(&start[row + x1 + 1]);
       for (uint32_t k = b; k < e; ++k) {
         float4 q = __ldg(&sorted[k]);
-        uint32_t wj = wbits(q);
-        int gj = (int)(wj >> BF_BITS);
-        if (abs(gi - gj) <= 1) continue;
-        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-        float d2 = dx * dx + dy * dy + dz * dz;
-        float cf = pair_coef<MODE>(d2, het && (wj & BF_HET), ff);
-        fx += cf * dx;
-        fy += cf * dy;
-        fz += cf * dz;
+        pair_accum<MODE>(p, wi, q, ff, acc);
       }
     }
   }
-  fs[slot] = make_float4(fx, fy, fz, 0.0f);
+  fs[slot] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
 // Cell-major pair kernel. One warp per cell; the warp's 4 groups of 8 lanes
@@ -474,51 +503,34 @@ constexpr int PAIR_NGROUPS = 32 / PAIR_GROUP;   // groups per warp
 constexpr int PAIR_HOME = 2 * PAIR_NGROUPS;     // home beads per warp pass
 
 template <int MODE>
-__device__ __forceinline__ void pair_accum(float4 p, uint32_t wi, float4 q, const ForceField &ff,
-                                           float3 &acc) {
-  uint32_t wj = wbits(q);
-  int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
-  if ((unsigned)(gi - gj + 1) <= 2u) return;  // |i - j| <= 1, self included
-  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-  float d2 = dx * dx + dy * dy + dz * dz;
-  bool hh = (wi & wj & BF_HET) != 0u;
-  float cf = pair_coef<MODE>(d2, hh, ff);
-  acc.x += cf * dx;
-  acc.y += cf * dy;
-  acc.z += cf * dz;
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(PAIR_WARPS * 32)
+__global__ void __launch_bounds__(PAIR_WARPS * 32, 4)
     k_pair_cells(const Tile *__restrict__ ctiles, const SysDesc *__restrict__ sys, ForceField ff,
                  const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                  float4 *__restrict__ fs) {
+  // cell starts of the 9 neighbour rows over x in [xb - 1, xb + PAIR_WARPS + 1],
+  // staged once for the CTA (all warps reach the barrier before any returns)
+  __shared__ uint32_t s_start[9][PAIR_WARPS + 4];
   Tile t = ctiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
   const int cps = s.cps;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if ((t.begin - s.cell_off) % cps + warp >= cps) return;  // beyond the row segment
-  const int c = t.begin + warp;                              // global cell index
-  const int lc = c - s.cell_off;
-  const int cx = lc % cps, cyz = lc / cps;
-  const int cy = cyz % cps, cz = cyz / cps;
-  const uint32_t hb = start[c], he = start[c + 1];
+  const int xb = (t.begin - s.cell_off) % cps, rowi = (t.begin - s.cell_off) / cps;
+  const int cy = rowi % cps, cz = rowi / cps;
+  for (int idx = threadIdx.x; idx < 9 * (PAIR_WARPS + 4); idx += blockDim.x) {
+    int r = idx / (PAIR_WARPS + 4), j = idx % (PAIR_WARPS + 4);
+    int y = cy + (r % 3) - 1, z = cz + (r / 3) - 1, xi = xb - 1 + j;
+    uint32_t v = 0;
+    if (y >= 0 && y < cps && z >= 0 && z < cps && xi >= 0 && xi <= cps)
+      v = start[s.cell_off + (z * cps + y) * cps + xi];  // xi = cps: end of the row
+    s_start[r][j] = v;
+  }
+  __syncthreads();
+  const int cx = xb + warp;
+  if (cx >= cps) return;  // beyond the row segment
+  const uint32_t hb = s_start[4][warp + 1], he = s_start[4][warp + 2];
   if (hb == he) return;
   // the 9 candidate ranges (x-adjacent cells of each (dy, dz) row)
-  uint32_t rb[9], rlen[9];
-  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, cps - 1);
-#pragma unroll
-  for (int r = 0; r < 9; ++r) {
-    int y = cy + (r % 3) - 1, z = cz + (r / 3) - 1;
-    uint32_t b = 0, e = 0;
-    if (y >= 0 && y < cps && z >= 0 && z < cps) {
-      int row = s.cell_off + (z * cps + y) * cps;
-      b = start[row + x0];
-      e = start[row + x1 + 1];
-    }
-    rb[r] = b;
-    rlen[r] = e - b;
-  }
+  const int j0 = max(cx - 1, 0) - (xb - 1), j1 = min(cx + 1, cps - 1) + 1 - (xb - 1);
   const int g = lane / PAIR_GROUP, gl = lane % PAIR_GROUP;
   for (uint32_t h0 = hb; h0 < he; h0 += PAIR_HOME) {
     const uint32_t ha = h0 + g, hc = h0 + g + PAIR_NGROUPS;
@@ -531,12 +543,15 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32)
     uint32_t k = gl;
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
-      for (; k < rlen[r]; k += PAIR_GROUP) {
-        float4 q = __ldg(&sorted[rb[r] + k]);
-        if (va) pair_accum<MODE>(pa, wa, q, ff, aa);
-        if (vc) pair_accum<MODE>(pc, wc, q, ff, ac);
+      const uint32_t rb = s_start[r][j0], rlen = s_start[r][j1] - rb;
+      for (; k < rlen; k += PAIR_GROUP) {
+        float4 q = __ldg(&sorted[rb + k]);
+        // both home slots are evaluated (an empty slot repeats bead hb and is
+        // discarded), so the groups of a warp never diverge
+        pair_accum<MODE>(pa, wa, q, ff, aa);
+        pair_accum<MODE>(pc, wc, q, ff, ac);
       }
-      k -= rlen[r];
+      k -= rlen;
     }
 #pragma unroll
     for (int o = PAIR_GROUP / 2; o > 0; o >>= 1) {
