@@ -92,19 +92,24 @@ def test_forces_baseline_match_fp64_oracle(base_sim, orc, steps):
     assert err <= FORCE_RTOL
 
 
-def test_pair_kernels_agree(ccp_sim, orc):
-    """The thread-per-bead and the warp-per-cell pair kernels give the same forces."""
+@pytest.mark.parametrize("kernel", [0, 1, 2])
+def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel):
+    """Full-shell thread-per-bead (0), warp-per-cell (1) and half-shell (2)
+    pair kernels all meet the force bound, for both presets."""
     from tfm_gb300.ccpgpu import ChrSim
 
     sim, R = ccp_sim
     txt, _, _ = ccp_params(2048, laf=0.3)
-    other = ChrSim(txt + "pair_kernel 1\n", seed=7)
-    other.set_types(sim.types())
-    other.set_lbs(sim.lbs())
-    other.set_positions(sim.positions())
-    (f64, sa), fl, geo = _oracle_forces(orc, sim, orc.ccp_ff(), 2.0, [0])
-    assert _force_ok(other.forces(), f64, sa) <= FORCE_RTOL
-    assert _force_ok(sim.forces(), f64, sa) <= FORCE_RTOL
+    for ref, text, ff, csl, heads in (
+            (sim, txt, orc.ccp_ff(), 2.0, [0]),
+            (base_sim, baseline_params(2048, "number_of_chains 4\n"), orc.baseline_ff(), 2.5,
+             [0, 512, 1024, 1536])):
+        other = ChrSim(text + "pair_kernel %d\n" % kernel, seed=7)
+        other.set_types(ref.types())
+        other.set_lbs(ref.lbs())
+        other.set_positions(ref.positions())
+        (f64, sa), fl, geo = _oracle_forces(orc, ref, ff, csl, heads)
+        assert _force_ok(other.forces(), f64, sa) <= FORCE_RTOL
 
 
 def _golden_cases():

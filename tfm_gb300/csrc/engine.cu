@@ -370,8 +370,9 @@ struct Engine {
   }
 
   void launch_scatter(const float4 *src) {
-    k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, src, rank.p,
-                                                             start.p, sorted.p, d_err.p);
+    k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+        d_tiles.p, d_sys.p, src, rank.p, start.p, sorted.p,
+        par.pair_kernel == 2 ? fs.p : nullptr, d_err.p);
     kcount += 1;
   }
 
@@ -380,6 +381,9 @@ struct Engine {
     if (par.pair_kernel == 0)
       k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                   start.p, fs.p);
+    else if (par.pair_kernel == 2)
+      k_pair_half<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                       sorted.p, start.p, fs.p);
     else
       k_pair_cells<MODE><<<(unsigned)hctiles.size(), PAIR_WARPS * 32, 0, stream>>>(
           d_ctiles.p, d_sys.p, ff, sorted.p, start.p, fs.p);

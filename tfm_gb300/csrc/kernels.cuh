@@ -397,12 +397,13 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
                           const float4 *__restrict__ src, const uint32_t *__restrict__ rank,
                           const uint32_t *__restrict__ start, float4 *__restrict__ sorted,
-                          int *__restrict__ err) {
+                          float4 *__restrict__ fs_clear, int *__restrict__ err) {
   Tile t = tiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
   int i = t.begin + threadIdx.x;
   int end = s.bead_off + s.n;
   if (i >= end) return;
+  if (fs_clear) fs_clear[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // for the half-shell pass
   bool esc = false;
   float4 p = src[i];
   int c = cell_linear(cell_of(p, s, esc), s);
@@ -482,11 +483,83 @@ __global__ void __launch_bounds__(128)
       uint32_t e = __ldg(&start[row + x1 + 1]);
       for (uint32_t k = b; k < e; ++k) {
         float4 q = __ldg(&sorted[k]);
-        pair_accum<MODE>(p, wi, q, ff, acc);
+        uint32_t wj = wbits(q);
+        int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
+        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        float d2 = dx * dx + dy * dy + dz * dz;
+        bool hh = (wi & wj & BF_HET) != 0u;
+        float rc = (MODE == MODE_ICG) ? ff.rc_icg : (hh ? ff.rc_att : ff.rc_rep);
+        if (d2 > rc * rc || (unsigned)(gi - gj + 1) <= 2u) continue;
+        float cf = pair_coef<MODE>(d2, hh, ff);
+        acc.x += cf * dx;
+        acc.y += cf * dy;
+        acc.z += cf * dz;
       }
     }
   }
   fs[slot] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+}
+
+// Half-shell pair kernel (Newton's third law). Each sorted bead i visits only
+// the forward half of its 27-cell neighbourhood: the beads after it in its own
+// cell and the +x cell (one contiguous range), the +y row of the same z layer,
+// and the three rows of the +z layer. Every pair is evaluated once; the force
+// on i accumulates in registers and the reaction on j is added to fs[j] with a
+// vector float4 atomic. fs must be zero on entry (the scatter clears it). Only
+// pairs inside the cutoff compute a coefficient and touch memory.
+template <int MODE>
+__device__ __forceinline__ void half_pair(float4 p, uint32_t wi, const float4 *__restrict__ sorted,
+                                          uint32_t k, const ForceField &ff, float3 &acc,
+                                          float4 *__restrict__ fs) {
+  float4 q = __ldg(&sorted[k]);
+  uint32_t wj = wbits(q);
+  int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
+  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  bool hh = (wi & wj & BF_HET) != 0u;
+  float rc = (MODE == MODE_ICG) ? ff.rc_icg : (hh ? ff.rc_att : ff.rc_rep);
+  if (d2 > rc * rc || (unsigned)(gi - gj + 1) <= 2u) return;
+  float cf = pair_coef<MODE>(d2, hh, ff);
+  float fx = cf * dx, fy = cf * dy, fz = cf * dz;
+  acc.x += fx;
+  acc.y += fy;
+  acc.z += fz;
+  atomicAdd(&fs[k], make_float4(-fx, -fy, -fz, 0.0f));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128)
+    k_pair_half(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
+                const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+                float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int slot = t.begin + threadIdx.x;
+  if (slot >= s.bead_off + s.n) return;
+  float4 p = sorted[slot];
+  uint32_t wi = wbits(p);
+  bool esc = false;
+  CellXYZ c = cell_of(p, s, esc);
+  const int cps = s.cps;
+  const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+  // own cell after i, then the +x cell
+  {
+    int row = s.cell_off + (c.z * cps + c.y) * cps;
+    uint32_t e = __ldg(&start[row + x1 + 1]);
+    for (uint32_t k = slot + 1; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
+  }
+  // +y row of this layer, then the 3 rows of the +z layer
+#pragma unroll 1
+  for (int r = 0; r < 4; ++r) {
+    int y = (r == 0) ? c.y + 1 : c.y + r - 2;
+    int z = (r == 0) ? c.z : c.z + 1;
+    if (y < 0 || y >= cps || z >= cps) continue;
+    int row = s.cell_off + (z * cps + y) * cps;
+    uint32_t b = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]);
+    for (uint32_t k = b; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
+  }
+  atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
 }
 
 // Cell-major pair kernel. One warp per cell; the warp's 4 groups of 8 lanes
