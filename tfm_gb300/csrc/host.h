@@ -71,7 +71,9 @@ struct Params {
   float packing_fraction = 0.2f;
   float lbs_area_fraction = 0.25f;
   bool relaxed = false;
-  int pair_kernel = 0;  // 0: thread per bead; 1: warp per cell (lane groups)
+  // 0: full shell, thread per bead; 1: warp per cell (lane groups);
+  // 2: half shell (Newton's third law), thread per bead
+  int pair_kernel = 2;
   std::string sequence_file = "Program/data/sequence.txt";
   ForceField ff{};
 };
