@@ -205,6 +205,40 @@ int ccpgpu_separation_counts(ccpgpu_sim *h, int32_t chain, int32_t *counts, doub
  * (chrsim::particle_overlaps, chrsim.cu:805-820). */
 int ccpgpu_overlaps(ccpgpu_sim *h, uint64_t *per_system, size_t n);
 
+/* ---------------------------------------------------------------- no allocation */
+
+/* Total force of one system evaluated without allocating device memory. No
+ * counterpart in the reference. It is for callers that cannot call cudaMalloc
+ * when they need forces: hosts whose own memory manager owns all of the GPU's
+ * memory, or time-critical loops where the device synchronisation of
+ * cudaMalloc/cudaFree would stall their other streams. The caller passes
+ * device buffers: d_xyz (3 floats per bead), d_types (ccp type codes) and
+ * d_forces (3 floats per bead, written), and the stream to run on (NULL: the
+ * legacy default stream). The result equals ccpgpu_compute_forces for the same
+ * system without lamina-binding sites (chain heads every n_beads / n_chains
+ * beads, the preset's default force field and cell grid).
+ *
+ * Scratch: a static device array of about 3.4 MB inside the library, held by
+ * every GPU that loads it until the process exits. Limits: n_beads <=
+ * CCPGPU_NOALLOC_MAX_BEADS and cells_per_side^3 <= CCPGPU_NOALLOC_MAX_CELLS;
+ * larger systems are rejected with CCPGPU_ERR_ARG. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture on that device. Every call uses the same array and
+ * it keeps the last call's contents: calls that overlap on the GPU (on
+ * different streams without ordering) race and corrupt each other. */
+#define CCPGPU_NOALLOC_MAX_BEADS 32768
+#define CCPGPU_NOALLOC_MAX_CELLS 131072
+
+typedef struct ccpgpu_noalloc_system {
+  int32_t preset;       /* 0 = ccp, 1 = baseline */
+  int32_t n_beads;      /* 3 .. CCPGPU_NOALLOC_MAX_BEADS */
+  int32_t n_chains;     /* equal chains */
+  float nucleus_radius; /* spherical nucleus */
+} ccpgpu_noalloc_system;
+
+int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sys, const float *d_xyz,
+                          const int32_t *d_types, float *d_forces, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,16 @@ SYMBOLS = (
     "ccpgpu_reset_observables", "ccpgpu_contact_counts", "ccpgpu_observable_sums",
     "ccpgpu_separation_counts", "ccpgpu_overlaps", "ccpgpu_advance", "ccpgpu_synchronize",
     "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
+    "ccpgpu_forces_noalloc",
 )
+
+NOALLOC_MAX_BEADS = 32768
+NOALLOC_MAX_CELLS = 131072
+
+
+class NoallocSystem(C.Structure):
+    _fields_ = [("preset", C.c_int32), ("n_beads", C.c_int32), ("n_chains", C.c_int32),
+                ("nucleus_radius", C.c_float)]
 
 
 class CcpError(RuntimeError):
@@ -106,6 +115,7 @@ def load(path=LIB_PATH):
         "ccpgpu_stream_handle": [P, C.POINTER(P)],
         "ccpgpu_kernel_times": [P, I32, P, SZ],
         "ccpgpu_kernel_count": [P, C.POINTER(C.c_uint64)],
+        "ccpgpu_forces_noalloc": [C.POINTER(NoallocSystem), P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -335,6 +345,21 @@ class ChrSim(_Handle):
 
         fn = FRAME_FN(cb)
         _check(_lib.ccpgpu_run_simulation(self._h, fn, None))
+
+
+def forces_noalloc(preset, n_beads, n_chains, nucleus_radius, d_xyz, d_types, d_forces,
+                   stream=0):
+    """ccpgpu_forces_noalloc on caller-owned device buffers (raw device
+    addresses as ints); allocates no device memory. Returns the status code."""
+    load()
+    s = NoallocSystem(int(preset), int(n_beads), int(n_chains), float(nucleus_radius))
+    return _lib.ccpgpu_forces_noalloc(C.byref(s), C.c_void_p(d_xyz), C.c_void_p(d_types),
+                                      C.c_void_p(d_forces), C.c_void_p(stream or None))
+
+
+def last_error():
+    load()
+    return _lib.ccpgpu_last_error().decode()
 
 
 def _trr_frame(i_f, t, xyz, n):

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -1226,3 +1227,171 @@ int ccpgpu_overlaps(ccpgpu_sim *h, uint64_t *per_system, size_t n) {
 }
 
 }  // extern "C"
+
+// ====================================================================== no-allocation forces
+//
+// Some callers cannot allocate device memory at the moment they need forces:
+// a host whose memory manager owns all of the GPU's memory and forbids foreign
+// cudaMalloc, or a time-critical loop where the implicit device
+// synchronisation of cudaMalloc/cudaFree would stall its other streams.
+// ccpgpu_forces_noalloc serves them: it evaluates the total force of one
+// system from caller-provided device buffers, and its cell list, cell-ordered
+// copy and force scratch live in one fixed static device array instead of
+// memory allocated per handle.
+
+namespace ccpgpu {
+namespace noalloc {
+
+constexpr int MAX_BEADS = CCPGPU_NOALLOC_MAX_BEADS;
+constexpr int MAX_CELLS = CCPGPU_NOALLOC_MAX_CELLS;
+constexpr int SCAN_CELLS = ((MAX_CELLS + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK) * SCAN_CHUNK;
+constexpr int SCAN_BLOCKS = SCAN_CELLS / SCAN_CHUNK;
+constexpr int MAX_TILES = (MAX_BEADS + TILE - 1) / TILE;
+
+// byte layout of the scratch array (each part 256-byte aligned)
+constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t OFF_POS = 0;
+constexpr size_t OFF_SORTED = OFF_POS + al(sizeof(float4) * (MAX_BEADS + 1));
+constexpr size_t OFF_FS = OFF_SORTED + al(sizeof(float4) * (MAX_BEADS + 1));
+constexpr size_t OFF_FOUT = OFF_FS + al(sizeof(float4) * (MAX_BEADS + 1));
+constexpr size_t OFF_RANK = OFF_FOUT + al(sizeof(float4) * (MAX_BEADS + 1));
+constexpr size_t OFF_COUNTS = OFF_RANK + al(sizeof(uint32_t) * (MAX_BEADS + 1));
+constexpr size_t OFF_START = OFF_COUNTS + al(sizeof(uint32_t) * SCAN_CELLS);
+constexpr size_t OFF_BSUM = OFF_START + al(sizeof(uint32_t) * (SCAN_CELLS + 4));
+constexpr size_t OFF_TILES = OFF_BSUM + al(sizeof(uint32_t) * (SCAN_BLOCKS + 1));
+constexpr size_t OFF_SYS = OFF_TILES + al(sizeof(Tile) * MAX_TILES);
+constexpr size_t OFF_STEP = OFF_SYS + al(sizeof(SysDesc));
+constexpr size_t OFF_ERR = OFF_STEP + al(sizeof(unsigned long long));
+constexpr size_t BYTES = OFF_ERR + al(sizeof(int) * ERR_COUNT);
+
+// The scratch: about 3.4 MB, held by every GPU that loads the library until
+// the process exits. Device code could name it directly; host code only knows
+// its host-side stand-in and obtains the device address per device below.
+static __device__ __align__(256) unsigned char scratch[BYTES];
+
+constexpr int MAX_DEVICES = 64;
+static std::mutex g_mutex;
+static unsigned char *g_base[MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device with that device current.
+static unsigned char *scratch_base(int dev) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_base[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, scratch);
+    if (e != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e));
+    g_base[dev] = static_cast<unsigned char *>(p);
+  }
+  return g_base[dev];
+}
+
+// Writes the system descriptor and the bead tiles of the single system.
+__global__ void k_na_setup(SysDesc d, Tile *tiles, SysDesc *sys, int n_tiles) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *sys = d;
+  if (i < n_tiles) tiles[i] = Tile{0, i * TILE};
+}
+
+// Packed xyz + ccp type codes -> float4 positions with the bead flags of the
+// preset; chain heads every L beads (equal chains).
+__global__ void k_na_pack(const float *__restrict__ xyz, const int32_t *__restrict__ pt, int n,
+                          int chain_len, int preset, float4 *__restrict__ pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  uint32_t f = BF_START;
+  float x = 0.0f, y = 0.0f, z = 0.0f;
+  if (i < n) {
+    f = 0u;
+    bool a = (pt[i] & 1) == 0;
+    if (a) f |= BF_HET;
+    if (preset == PRESET_CCP ? a : ((pt[i] & 2) != 0)) f |= BF_LAD;
+    if (i % chain_len == 0) f |= BF_START;
+    x = xyz[3 * i];
+    y = xyz[3 * i + 1];
+    z = xyz[3 * i + 2];
+  }
+  pos[i] = make_float4(x, y, z, __uint_as_float(f));
+}
+
+}  // namespace noalloc
+}  // namespace ccpgpu
+
+extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const float *d_xyz,
+                                     const int32_t *d_types, float *d_forces, void *stream) {
+  using namespace ccpgpu::noalloc;
+  return guarded([&] {
+    need(sysp && d_xyz && d_types && d_forces, "null argument");
+    const ccpgpu_noalloc_system a = *sysp;
+    need(a.preset == PRESET_CCP || a.preset == PRESET_BASELINE, "preset out of range");
+    if (!(a.n_beads >= 3 && a.n_beads <= MAX_BEADS))
+      throw Error(ST_ARG, "n_beads outside 3.." + std::to_string(MAX_BEADS) +
+                              " (the no-allocation scratch limit)");
+    need(a.n_chains >= 1 && a.n_chains <= a.n_beads, "bad chain count");
+    need(a.nucleus_radius > 1.0f, "nucleus radius too small");
+    // the preset force field and cell grid (as parse_params sets them)
+    ForceField ff = make_preset(a.preset);
+    const float csl = (a.preset == PRESET_CCP) ? CCP_ACO : std::max(ff.rc_att, 1.5f);
+    Geometry g = make_geometry(a.nucleus_radius, 0.0f, 0.0f);
+    SysDesc d{};
+    d.bead_off = 0;
+    d.n = a.n_beads;
+    d.csl = csl;
+    d.inv_csl = 1.0f / csl;
+    d.cps = std::max(2, 2 * (int)std::ceil(g.d_m / csl));
+    long long cells = (long long)d.cps * d.cps * d.cps;
+    if (cells > MAX_CELLS)
+      throw Error(ST_ARG, "cell grid of " + std::to_string(cells) + " cells exceeds the " +
+                              std::to_string(MAX_CELLS) + "-cell no-allocation limit");
+    d.cell_off = 0;
+    d.R_n = g.R_n;
+    d.R_o = g.R_o;
+    d.R_b = g.R_b;
+    d.noc = g.noc;
+    d.boc = g.boc;
+    d.nod = g.nod;
+    d.bod = g.bod;
+    d.n_lbs = 0;
+    d.lbs_rmin = 1e30f;
+    d.lbs_rmax = -1e30f;
+    d.n_chains = a.n_chains;
+    const int nc = (int)cells;
+    const int nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    const int n_tiles = (a.n_beads + TILE - 1) / TILE;
+
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    need(dev >= 0 && dev < MAX_DEVICES, "device index out of range");
+    unsigned char *base = scratch_base(dev);
+    float4 *pos = reinterpret_cast<float4 *>(base + OFF_POS);
+    float4 *sorted = reinterpret_cast<float4 *>(base + OFF_SORTED);
+    float4 *fs = reinterpret_cast<float4 *>(base + OFF_FS);
+    float4 *fout = reinterpret_cast<float4 *>(base + OFF_FOUT);
+    uint32_t *rank = reinterpret_cast<uint32_t *>(base + OFF_RANK);
+    uint32_t *counts = reinterpret_cast<uint32_t *>(base + OFF_COUNTS);
+    uint32_t *start = reinterpret_cast<uint32_t *>(base + OFF_START);
+    uint32_t *bsum = reinterpret_cast<uint32_t *>(base + OFF_BSUM);
+    Tile *tiles = reinterpret_cast<Tile *>(base + OFF_TILES);
+    SysDesc *sys = reinterpret_cast<SysDesc *>(base + OFF_SYS);
+    unsigned long long *step = reinterpret_cast<unsigned long long *>(base + OFF_STEP);
+    int *err = reinterpret_cast<int *>(base + OFF_ERR);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // the array keeps the previous call's contents: clear what must start at zero
+    CK(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (size_t)nblk * SCAN_CHUNK, s));
+    CK(cudaMemsetAsync(err, 0, sizeof(int) * ERR_COUNT, s));
+    k_na_setup<<<(n_tiles + 127) / 128, 128, 0, s>>>(d, tiles, sys, n_tiles);
+    k_na_pack<<<(a.n_beads + 1 + 255) / 256, 256, 0, s>>>(
+        d_xyz, d_types, a.n_beads, std::max(1, a.n_beads / a.n_chains), a.preset, pos);
+    k_count<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, counts, rank, err);
+    k_scan_reduce<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum);
+    k_scan_top<<<1, SCAN_TOP_THREADS, 0, s>>>(bsum, nblk, step, 0);
+    k_scan_apply<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum, start, nc, nblk);
+    k_scatter<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, rank, start, sorted, fs, err);
+    k_pair_half<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, sorted, start, fs);
+    k_total_force<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, pos, fs, rank, start,
+                                                     nullptr, nullptr, fout);
+    k_pack_xyz<<<(a.n_beads + 255) / 256, 256, 0, s>>>(fout, d_forces, a.n_beads);
+    CK(cudaGetLastError());
+  });
+}

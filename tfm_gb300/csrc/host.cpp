@@ -121,6 +121,10 @@ static ForceField preset_baseline(float kT, float dt) {
   return f;
 }
 
+ForceField make_preset(int preset) {
+  return preset == PRESET_CCP ? preset_ccp(298.0f) : preset_baseline(1.0f, 1.0e-3f);
+}
+
 Params parse_params(const std::string &text) {
   ParamMap pm(text);
   Params p;

@@ -82,6 +82,10 @@ struct Params {
 // chrsim.cu:421-435). Throws Error(ST_PARAM, ccp's message).
 Params parse_params(const std::string &text);
 
+// Force field of a preset with its default temperature and time step (ccp:
+// T = 298 K, dt = 1/2048; baseline: kT = 1, dt = 1e-3); allocates nothing.
+ForceField make_preset(int preset);
+
 // One independent system of a batch.
 struct SystemSpec {
   int n = 0;
