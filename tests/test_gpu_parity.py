@@ -92,10 +92,11 @@ def test_forces_baseline_match_fp64_oracle(base_sim, orc, steps):
     assert err <= FORCE_RTOL
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2])
-def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel):
+@pytest.mark.parametrize("kernel,half_cells", [(0, False), (1, False), (2, False), (2, True)])
+def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel, half_cells):
     """Full-shell thread-per-bead (0), warp-per-cell (1) and half-shell (2)
-    pair kernels all meet the force bound, for both presets."""
+    pair kernels, the last also on cells of half the cutoff (5x5x5
+    neighbourhood), all meet the force bound, for both presets."""
     from tfm_gb300.ccpgpu import ChrSim
 
     sim, R = ccp_sim
@@ -104,7 +105,10 @@ def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel):
             (sim, txt, orc.ccp_ff(), 2.0, [0]),
             (base_sim, baseline_params(2048, "number_of_chains 4\n"), orc.baseline_ff(), 2.5,
              [0, 512, 1024, 1536])):
-        other = ChrSim(text + "pair_kernel %d\n" % kernel, seed=7)
+        extra = "pair_kernel %d\n" % kernel
+        if half_cells:
+            extra += "cell_side %r\n" % (csl / 2)
+        other = ChrSim(text + extra, seed=7)
         other.set_types(ref.types())
         other.set_lbs(ref.lbs())
         other.set_positions(ref.positions())
@@ -176,6 +180,25 @@ def test_contact_map_bit_exact_vs_reference(engine_lib, orc, path):
     ref = np.zeros(int(g["cm_len"]), np.float32)
     ref[g["cm_idx"]] = g["cm_val"]
     assert np.array_equal(val.astype(np.float32), ref)
+
+
+def test_contacts_on_half_cells_bit_exact(engine_lib, orc):
+    """Contact counts from the 5x5x5 neighbourhood (cells of half the cutoff)
+    equal the oracle's all-pairs counts."""
+    from tfm_gb300.ccpgpu import ChrSim
+
+    txt, R, n_l = ccp_params(2048)
+    sim = ChrSim(txt + "cell_side 1.0\n", seed=9)
+    sim.generate_initial_condition()
+    sim.run_steps(500)
+    sim.reset_observables()
+    sim.observe()
+    si = sim.system_info(0)
+    m, ps, ps_off = orc.contacts(sim.positions(), 2.0, si.contact_bins, si.map_len, si.copy_len,
+                                 si.n_copies, [0])
+    assert np.array_equal(sim.contact_counts(0), m)
+    cc, _ = sim.separation_counts(0, 2048)
+    assert np.array_equal(cc, ps[:len(cc)])
 
 
 @pytest.mark.parametrize("path", _golden_cases(), ids=os.path.basename)

@@ -382,6 +382,9 @@ struct Engine {
     if (par.pair_kernel == 0)
       k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                   start.p, fs.p);
+    else if (par.pair_kernel == 2 && par.reach == 2)
+      k_pair_half<MODE, 2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                          sorted.p, start.p, fs.p);
     else if (par.pair_kernel == 2)
       k_pair_half<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                        sorted.p, start.p, fs.p);
@@ -417,11 +420,17 @@ struct Engine {
   }
 
   // Observables on the cell-ordered copy of pos (must be current).
-  void launch_contacts() {
-    k_contacts<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p, start.p,
-                                                              contact_args(true, true, false));
+  void launch_contacts_args(const ContactArgs &a) {
+    if (par.reach == 2)
+      k_contacts<2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                    start.p, a);
+    else
+      k_contacts<1><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                    start.p, a);
     kcount += 1;
   }
+
+  void launch_contacts() { launch_contacts_args(contact_args(true, true, false)); }
 
   void launch_observe() {
     k_observe<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p,
@@ -613,8 +622,7 @@ struct Engine {
   std::vector<unsigned long long> overlaps() {
     CK(cudaMemsetAsync(ovl.p, 0, sizeof(unsigned long long) * hsys.size(), stream));
     sort_now();
-    k_contacts<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p, start.p,
-                                                              contact_args(false, false, true));
+    launch_contacts_args(contact_args(false, false, true));
     recount();
     CK(cudaGetLastError());
     std::vector<unsigned long long> o(hsys.size());

@@ -220,7 +220,15 @@ Params parse_params(const std::string &text) {
   float need = std::max({p.ff.rc_att, p.ff.rc_rep, p.ff.rc_icg, p.contact_cutoff, p.ff.mis});
   float def_cs = (p.preset == PRESET_CCP) ? CCP_ACO : need;
   p.cell_side = pm.get<float>("cell_side", std::max(def_cs, need));
-  if (!(p.cell_side >= need && p.cell_side < 1.0e3f)) fail("cell_side below interaction cutoff");
+  // cells of at least the largest cutoff use the 3x3x3 neighbourhood; cells of
+  // at least half of it the 5x5x5 one (half-shell pair kernel only)
+  if (!(p.cell_side < 1.0e3f)) fail("cell_side below interaction cutoff");
+  if (p.cell_side >= need)
+    p.reach = 1;
+  else if (p.cell_side >= 0.5f * need && p.pair_kernel == 2)
+    p.reach = 2;
+  else
+    fail("cell_side below interaction cutoff");
   return p;
 }
 

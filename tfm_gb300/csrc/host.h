@@ -66,6 +66,7 @@ struct Params {
   float contact_cutoff = CCP_ACO;
   int contact_bins = 0;  // 0: ccp pixels of 4 beads
   float cell_side = 0;   // 0: automatic
+  int reach = 1;         // neighbour cells per axis: cell_side >= cutoff / reach
   float lad_fraction = 0.1f;
   float mean_block = 16.0f;
   float packing_fraction = 0.2f;

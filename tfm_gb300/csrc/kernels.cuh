@@ -527,7 +527,11 @@ __device__ __forceinline__ void half_pair(float4 p, uint32_t wi, const float4 *_
   atomicAdd(&fs[k], make_float4(-fx, -fy, -fz, 0.0f));
 }
 
-template <int MODE>
+// REACH = 1: cells of side >= the largest cutoff, 3x3x3 neighbourhood.
+// REACH = 2: cells of side >= half of it, 5x5x5 neighbourhood: the candidate
+// volume drops from 27 to 15.6 cutoff-cubes (x0.58) at the price of 13 instead
+// of 5 row ranges per bead.
+template <int MODE, int REACH = 1>
 __global__ void __launch_bounds__(128)
     k_pair_half(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
@@ -541,19 +545,27 @@ __global__ void __launch_bounds__(128)
   bool esc = false;
   CellXYZ c = cell_of(p, s, esc);
   const int cps = s.cps;
-  const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
+  const int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
   float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-  // own cell after i, then the +x cell
+  // own cell after i, then the +x cells
   {
     int row = s.cell_off + (c.z * cps + c.y) * cps;
     uint32_t e = __ldg(&start[row + x1 + 1]);
     for (uint32_t k = slot + 1; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
   }
-  // +y row of this layer, then the 3 rows of the +z layer
+  // the +y rows of this layer, then all rows of the +z layers
+  constexpr int NR = REACH + REACH * (2 * REACH + 1);
 #pragma unroll 1
-  for (int r = 0; r < 4; ++r) {
-    int y = (r == 0) ? c.y + 1 : c.y + r - 2;
-    int z = (r == 0) ? c.z : c.z + 1;
+  for (int r = 0; r < NR; ++r) {
+    int y, z;
+    if (r < REACH) {
+      y = c.y + 1 + r;
+      z = c.z;
+    } else {
+      int q = r - REACH;
+      y = c.y - REACH + q % (2 * REACH + 1);
+      z = c.z + 1 + q / (2 * REACH + 1);
+    }
     if (y < 0 || y >= cps || z >= cps) continue;
     int row = s.cell_off + (z * cps + y) * cps;
     uint32_t b = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]);
@@ -914,6 +926,8 @@ struct ContactArgs {
 // cell-ordered copy: binned contact map (calc_cm, chrana.cu:48-84), per-chain
 // contact counts by separation (the cp part of calc_sd_cp, chrana.cu:13-45) and
 // the overlap count of the initial-condition relaxation (chrsim.cu:805-820).
+// REACH as for the pair kernel (cells of side >= cutoff / REACH).
+template <int REACH = 1>
 __global__ void __launch_bounds__(128)
     k_contacts(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
                const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
@@ -934,9 +948,9 @@ __global__ void __launch_bounds__(128)
     bool esc = false;
     CellXYZ c = cell_of(p, s, esc);
     const int cps = s.cps;
-    int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, cps - 1);
-    for (int z = max(c.z - 1, 0); z <= min(c.z + 1, cps - 1); ++z)
-      for (int y = max(c.y - 1, 0); y <= min(c.y + 1, cps - 1); ++y) {
+    int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
+    for (int z = max(c.z - REACH, 0); z <= min(c.z + REACH, cps - 1); ++z)
+      for (int y = max(c.y - REACH, 0); y <= min(c.y + REACH, cps - 1); ++y) {
         int row = s.cell_off + (z * cps + y) * cps;
         uint32_t b = start[row + x0], e = start[row + x1 + 1];
         for (uint32_t k = b; k < e; ++k) {
