@@ -994,31 +994,50 @@ constexpr int N_SHELLS = 64;  // radial bins (chrana.cuh:16)
 // density volumes (A, B, all) of chrana.cu:422-480.
 constexpr int OBS_STRIDE = 4 + 3 * N_SHELLS;
 
-__global__ void __launch_bounds__(128)
+// Each warp accumulates the shell volumes of its 32 beads in its own FP32
+// shared histogram (native shared float atomics; a bead near the wall spans up
+// to ~20 thin outer shells); the position sums for Rg^2 are reduced in FP64 by
+// warp shuffles. The CTA then folds the warp histograms into FP64 and adds the
+// non-zero entries to the system's accumulators.
+constexpr int OBS_WARPS = 4;
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(OBS_WARPS * 32)
     k_observe(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
               const float4 *__restrict__ pos, float bead_r, double *__restrict__ acc) {
-  __shared__ double sh[OBS_STRIDE];
+  __shared__ float hist[OBS_WARPS][3 * N_SHELLS];
+  __shared__ double sums[4];
   __shared__ float rb[N_SHELLS];
   Tile t = tiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
-  for (int k = threadIdx.x; k < OBS_STRIDE; k += blockDim.x) sh[k] = 0.0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int k = threadIdx.x; k < OBS_WARPS * 3 * N_SHELLS; k += blockDim.x) (&hist[0][0])[k] = 0.0f;
+  if (threadIdx.x < 4) sums[threadIdx.x] = 0.0;
   for (int k = threadIdx.x; k < N_SHELLS; k += blockDim.x)
     rb[k] = s.R_n * cbrtf((k + 1.0f) / N_SHELLS);
   __syncthreads();
   int i = t.begin + threadIdx.x;
+  double px = 0.0, py = 0.0, pz = 0.0;
   if (i < s.bead_off + s.n) {
     float4 p = pos[i];
     bool het = (wbits(p) & BF_HET) != 0u;
-    double px = p.x, py = p.y, pz = p.z;
-    atomicAdd(&sh[0], px);
-    atomicAdd(&sh[1], py);
-    atomicAdd(&sh[2], pz);
-    atomicAdd(&sh[3], px * px + py * py + pz * pz);
+    px = p.x;
+    py = p.y;
+    pz = p.z;
     float dr = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
     const float a = bead_r;
     const float vfull = (4.0f / 3.0f) * 3.14159265358979f * a * a * a;
+    // first shell that can overlap the bead (a few below the estimate)
+    float inner = fmaxf(dr - a, 0.0f) / s.R_n;
+    int b0 = max(0, (int)floorf(N_SHELLS * inner * inner * inner) - 2);
     float vprev = 0.0f;
-    for (int b = 0; b < N_SHELLS; ++b) {
+    float *h = hist[warp];
+    for (int b = b0; b < N_SHELLS; ++b) {
       float r = rb[b], v;
       if (dr - a > r) {
         v = 0.0f;
@@ -1034,16 +1053,29 @@ __global__ void __launch_bounds__(128)
       float dv = v - vprev;
       vprev = v;
       if (dv != 0.0f) {
-        atomicAdd(&sh[4 + (het ? 0 : 1) * N_SHELLS + b], (double)dv);
-        atomicAdd(&sh[4 + 2 * N_SHELLS + b], (double)dv);
+        atomicAdd(&h[(het ? 0 : 1) * N_SHELLS + b], dv);
+        atomicAdd(&h[2 * N_SHELLS + b], dv);
       }
-      if (v == vfull && dr + a < r) break;  // all further shells contribute zero
+      if (dr + a < r) break;  // bead inside shell b: all further shells get zero
     }
+  }
+  double sx = warp_sum_d(px), sy = warp_sum_d(py), sz = warp_sum_d(pz);
+  double sr = warp_sum_d(px * px + py * py + pz * pz);
+  if (lane == 0) {
+    atomicAdd(&sums[0], sx);
+    atomicAdd(&sums[1], sy);
+    atomicAdd(&sums[2], sz);
+    atomicAdd(&sums[3], sr);
   }
   __syncthreads();
   double *dst = acc + (size_t)t.sys * OBS_STRIDE;
-  for (int k = threadIdx.x; k < OBS_STRIDE; k += blockDim.x)
-    if (sh[k] != 0.0) atomicAdd(&dst[k], sh[k]);
+  if (threadIdx.x < 4 && sums[threadIdx.x] != 0.0) atomicAdd(&dst[threadIdx.x], sums[threadIdx.x]);
+  for (int k = threadIdx.x; k < 3 * N_SHELLS; k += blockDim.x) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < OBS_WARPS; ++w) v += (double)hist[w][k];
+    if (v != 0.0) atomicAdd(&dst[4 + k], v);
+  }
 }
 
 // Mean spatial distance by separation (the sd part of calc_sd_cp,
