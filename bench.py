@@ -35,6 +35,9 @@ PARAMS = ("force_field baseline\ncontact_bins 256\ncontact_cutoff 1.5\n"
 HEUN_PER_STEP = 100
 B_ALG = 192.0  # algorithmic HBM bytes per bead-step of a Heun step (2 force evaluations)
 PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4 force
+# DRAM bytes per bead of one pair launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on this workload: profiles/k_pair_half_c2.md
+PAIR_TRAFFIC_PER_BEAD = 47.1
 METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
 
 
@@ -273,15 +276,7 @@ def engine_arm(args, ws, rank, local):
     hbm, peak_kind = peaks()
     pair_s = kt["pair"] / 1000.0
     achieved = total * PAIR_BYTES / pair_s / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "pair_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as f:
-                tp = json.load(f)
-            traffic = tp["bytes_per_bead"] * total
-        except Exception:
-            traffic = None
+    traffic = PAIR_TRAFFIC_PER_BEAD * total if args.replicas == 512 else None
 
     # end to end through the C ABI with host buffers
     x = b.positions()
