@@ -92,7 +92,8 @@ def test_forces_baseline_match_fp64_oracle(base_sim, orc, steps):
     assert err <= FORCE_RTOL
 
 
-@pytest.mark.parametrize("kernel,half_cells", [(0, False), (1, False), (2, False), (2, True)])
+@pytest.mark.parametrize("kernel,half_cells",
+                         [(0, False), (1, False), (2, False), (2, True), (3, False), (3, True)])
 def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel, half_cells):
     """Full-shell thread-per-bead (0), warp-per-cell (1) and half-shell (2)
     pair kernels, the last also on cells of half the cutoff (5x5x5

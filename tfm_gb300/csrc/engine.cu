@@ -373,7 +373,7 @@ struct Engine {
   void launch_scatter(const float4 *src) {
     k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(
         d_tiles.p, d_sys.p, src, rank.p, start.p, sorted.p,
-        par.pair_kernel == 2 ? fs.p : nullptr, d_err.p);
+        par.pair_kernel >= 2 ? fs.p : nullptr, d_err.p);
     kcount += 1;
   }
 
@@ -382,6 +382,12 @@ struct Engine {
     if (par.pair_kernel == 0)
       k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                   start.p, fs.p);
+    else if (par.pair_kernel == 3 && par.reach == 2)
+      k_pair_flat<MODE, 2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                          sorted.p, start.p, fs.p);
+    else if (par.pair_kernel == 3)
+      k_pair_flat<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                       sorted.p, start.p, fs.p);
     else if (par.pair_kernel == 2 && par.reach == 2)
       k_pair_half<MODE, 2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                           sorted.p, start.p, fs.p);

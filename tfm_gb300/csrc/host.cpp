@@ -211,7 +211,7 @@ Params parse_params(const std::string &text) {
   p.mean_block = pm.get<float>("mean_block_length", 16.0f);
   p.sequence_file = pm.get<std::string>("sequence_file", p.sequence_file);
   p.pair_kernel = pm.get<int>("pair_kernel", 2);
-  if (!(p.pair_kernel >= 0 && p.pair_kernel <= 2)) fail("pair_kernel out of range");
+  if (!(p.pair_kernel >= 0 && p.pair_kernel <= 3)) fail("pair_kernel out of range");
   if (!(p.n_chains >= 1 && (uint32_t)p.n_chains <= p.N)) fail("number_of_chains out of range");
   if (!(p.contact_cutoff > 0.0f)) fail("contact_cutoff out of range");
   if (p.contact_bins < 0) fail("contact_bins out of range");
@@ -220,14 +220,14 @@ Params parse_params(const std::string &text) {
   float need = std::max({p.ff.rc_att, p.ff.rc_rep, p.ff.rc_icg, p.contact_cutoff, p.ff.mis});
   // ccp: its grid of side aco (chrsim.cu:425); baseline: cells of half the
   // largest cutoff with the 5x5x5 half-shell stencil (measured fastest on GB300)
-  float def_cs = (p.preset == PRESET_CCP) ? CCP_ACO : (p.pair_kernel == 2 ? 0.5f * need : need);
+  float def_cs = (p.preset == PRESET_CCP) ? CCP_ACO : (p.pair_kernel >= 2 ? 0.5f * need : need);
   p.cell_side = pm.get<float>("cell_side", def_cs);
   // cells of at least the largest cutoff use the 3x3x3 neighbourhood; cells of
   // at least half of it the 5x5x5 one (half-shell pair kernel only)
   if (!(p.cell_side < 1.0e3f)) fail("cell_side below interaction cutoff");
   if (p.cell_side >= need)
     p.reach = 1;
-  else if (p.cell_side >= 0.5f * need && p.pair_kernel == 2)
+  else if (p.cell_side >= 0.5f * need && p.pair_kernel >= 2)
     p.reach = 2;
   else
     fail("cell_side below interaction cutoff");

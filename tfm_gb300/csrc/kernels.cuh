@@ -574,6 +574,64 @@ __global__ void __launch_bounds__(128)
   atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
 }
 
+// Half-shell pair kernel with a flattened candidate walk: each lane runs one
+// loop over its whole candidate stream and fetches the next row range only
+// when the current one is exhausted, so a warp pays the longest total stream
+// of its lanes instead of the sum over rows of the longest row.
+template <int REACH>
+__device__ __forceinline__ void half_row(const SysDesc &s, CellXYZ c, int r, int x0, int x1,
+                                         const uint32_t *__restrict__ start, uint32_t &b,
+                                         uint32_t &e) {
+  int y, z;
+  if (r < REACH) {
+    y = c.y + 1 + r;
+    z = c.z;
+  } else {
+    int q = r - REACH;
+    y = c.y - REACH + q % (2 * REACH + 1);
+    z = c.z + 1 + q / (2 * REACH + 1);
+  }
+  b = e = 0;
+  if (y < 0 || y >= s.cps || z >= s.cps) return;
+  int row = s.cell_off + (z * s.cps + y) * s.cps;
+  b = __ldg(&start[row + x0]);
+  e = __ldg(&start[row + x1 + 1]);
+}
+
+template <int MODE, int REACH = 1>
+__global__ void __launch_bounds__(128)
+    k_pair_flat(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
+                const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+                float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int slot = t.begin + threadIdx.x;
+  if (slot >= s.bead_off + s.n) return;
+  float4 p = sorted[slot];
+  uint32_t wi = wbits(p);
+  bool esc = false;
+  CellXYZ c = cell_of(p, s, esc);
+  const int cps = s.cps;
+  const int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
+  constexpr int NR = REACH + REACH * (2 * REACH + 1);
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+  // range 0: own cell after i and the +x cells
+  uint32_t b = slot + 1;
+  uint32_t e = __ldg(&start[s.cell_off + (c.z * cps + c.y) * cps + x1 + 1]);
+  int r = 0;
+  for (;;) {
+    while (b >= e) {
+      if (r >= NR) goto done;
+      half_row<REACH>(s, c, r, x0, x1, start, b, e);
+      ++r;
+    }
+    half_pair<MODE>(p, wi, sorted, b, ff, acc, fs);
+    ++b;
+  }
+done:
+  atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
+}
+
 // Cell-major pair kernel. One warp per cell; the warp's 4 groups of 8 lanes
 // each own up to 2 of the cell's beads per pass, and the 8 lanes of a group
 // sweep the cell's 27-cell neighbourhood (9 x-contiguous ranges of the sorted
