@@ -240,6 +240,7 @@ def engine_arm(args, ws, rank, local):
     seeds = np.arange(args.replicas, dtype=np.uint64) + 1 + 100000 * rank
     b = Batch(PARAMS, sizes, seeds=seeds)
     b.generate_initial_condition()
+    tune = b.autotune(reps=3) if not args.no_tune else None  # per size class, untimed
     total = int(sizes.sum())
     stream = torch.cuda.ExternalStream(b.stream())
 
@@ -306,7 +307,11 @@ def engine_arm(args, ws, rank, local):
                                    % args.replicas,
                        "total_beads": total, "heun_steps_per_step": HEUN_PER_STEP,
                        "l2": "state (~%d MB) larger than the 129 MB L2" % (total * 100 // 2**20),
-                       "parallelism": "replicas per GPU (no collective)"},
+                       "parallelism": "replicas per GPU (no collective)",
+                       "autotune": None if tune is None else {
+                           "tile": tune["tile"],
+                           "cell_side_by_class": [[c["n_min"], c["n_max"], c["cell_side"]]
+                                                  for c in tune["classes"]]}},
             "clocks": clk,
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": "pair", "achieved": achieved, "peak": hbm,
@@ -393,6 +398,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

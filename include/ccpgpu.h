@@ -138,6 +138,15 @@ int ccpgpu_stream_handle(ccpgpu_sim *h, void **stream);
  * [6] observe. Leaves the simulation state advanced by reps steps. */
 int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n);
 
+/* Autotuner (no reference counterpart): per size class of the batch (bead
+ * counts in [2^k, 2^(k+1))) it times cell sides of 1, 0.75, 0.625, 0.55 and 0.5
+ * times the largest cutoff (the last four with the 5x5x5 stencil), keeps the
+ * fastest per class, then picks the per-bead tile size (64, 128, 256). Each
+ * candidate runs reps steps; positions, time and the noise counter are
+ * restored afterwards. report receives a NUL-terminated JSON summary (size in
+ * *len; CCPGPU_ERR_IO when cap is too small, after tuning). */
+int ccpgpu_autotune(ccpgpu_sim *h, int32_t reps, char *report, size_t cap, size_t *len);
+
 /* Number of engine kernels launched since creation (graph nodes included). */
 int ccpgpu_kernel_count(const ccpgpu_sim *h, uint64_t *count);
 

@@ -299,6 +299,33 @@ def test_batch_matches_single_systems(engine_lib):
         off += n
 
 
+def test_autotune_keeps_state_and_forces(engine_lib, orc):
+    """The autotuner re-grids size classes and picks a tile size without
+    changing positions or time, and forces stay within the bound afterwards."""
+    from tfm_gb300.ccpgpu import Batch
+
+    sizes = [1100, 1500, 2600, 3000, 5000]
+    b = Batch("force_field baseline\ncontact_bins 64\n", sizes, seeds=[1, 2, 3, 4, 5])
+    b.generate_initial_condition()
+    b.run_steps(100)
+    x0, step0 = b.positions(), b.info().step
+    rep = b.autotune(reps=3)
+    assert len(rep["classes"]) == 3 and rep["tile"] in (64, 128, 256)
+    assert np.array_equal(b.positions(), x0) and b.info().step == step0
+    f = b.forces()
+    pt, lbs = b.types(), b.lbs()
+    for s in range(len(sizes)):
+        si = b.system_info(s)
+        sl = slice(si.bead_offset, si.bead_offset + si.n_beads)
+        fl = orc.flags_from_types(pt[sl], [0], "baseline")
+        geo = orc.geo_vec(si.nucleus_radius, csl=2.5)
+        f64, sa = orc.forces(x0[sl], fl, lbs[si.lbs_offset:si.lbs_offset + si.n_lbs],
+                             orc.baseline_ff(), geo, with_abs=True, cells=True)
+        assert _force_ok(f[sl], f64, sa) <= FORCE_RTOL
+    b.run_steps(200)
+    assert np.isfinite(b.positions()).all()
+
+
 def test_checkpoint_roundtrip_and_resume(ccp_sim, engine_lib):
     from tfm_gb300.ccpgpu import ChrSim
 

@@ -32,7 +32,7 @@ SYMBOLS = (
     "ccpgpu_reset_observables", "ccpgpu_contact_counts", "ccpgpu_observable_sums",
     "ccpgpu_separation_counts", "ccpgpu_overlaps", "ccpgpu_advance", "ccpgpu_synchronize",
     "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
-    "ccpgpu_forces_noalloc",
+    "ccpgpu_forces_noalloc", "ccpgpu_autotune",
 )
 
 NOALLOC_MAX_BEADS = 32768
@@ -116,6 +116,7 @@ def load(path=LIB_PATH):
         "ccpgpu_kernel_times": [P, I32, P, SZ],
         "ccpgpu_kernel_count": [P, C.POINTER(C.c_uint64)],
         "ccpgpu_forces_noalloc": [C.POINTER(NoallocSystem), P, P, P, P],
+        "ccpgpu_autotune": [P, I32, P, SZ, C.POINTER(SZ)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -230,6 +231,15 @@ class _Handle:
         a = np.zeros(7, np.float64)
         _check(_lib.ccpgpu_kernel_times(self._h, int(reps), _ptr(a), a.size))
         return dict(zip(self.KERNELS, a.tolist()))
+
+    def autotune(self, reps=5):
+        """Per-size-class cell side and tile size by timing; returns the report."""
+        import json
+
+        n = C.c_size_t()
+        buf = C.create_string_buffer(1 << 16)
+        _check(_lib.ccpgpu_autotune(self._h, int(reps), buf, len(buf), C.byref(n)))
+        return json.loads(buf.value.decode())
 
     def kernel_count(self):
         c = C.c_uint64()

@@ -78,7 +78,7 @@ struct SysDesc {
   int64_t map_off;
   int32_t nbins, map_len, copy_len, n_copies;
   int32_t sys_index;
-  int32_t pad_;
+  int32_t reach;  // neighbour cells per axis (1: csl >= cutoff, 2: csl >= cutoff / 2)
 };
 
 // ---------------------------------------------------------------- Philox

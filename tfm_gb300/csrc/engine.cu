@@ -16,6 +16,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -64,6 +65,8 @@ struct Engine {
   std::vector<Tile> hctiles;  // cell tiles: PAIR_WARPS cells of one x-row
   int nb = 0, nc = 0, nl = 0, nch = 0;
   int nblk = 0;        // scan CTAs
+  int tile = TILE;     // beads per CTA of the per-bead kernels (64, 128 or 256)
+  float need_cut = 0;  // largest interaction / contact cutoff: cell side >= need_cut / reach
   int64_t map_total = 0;
   int ps_total = 0;
 
@@ -196,16 +199,9 @@ struct Engine {
       nc += d.cps * d.cps * d.cps;
       nl += q.n_lbs;
     }
-    htiles.clear();
-    for (int s = 0; s < ns; ++s)
-      for (int b = 0; b < hsys[s].n; b += TILE) htiles.push_back(Tile{s, hsys[s].bead_off + b});
-    hctiles.clear();
-    for (int s = 0; s < ns; ++s) {
-      const int cps = hsys[s].cps;
-      for (int row = 0; row < cps * cps; ++row)
-        for (int x = 0; x < cps; x += PAIR_WARPS)
-          hctiles.push_back(Tile{s, hsys[s].cell_off + row * cps + x});
-    }
+    need_cut = std::max({ff.rc_att, ff.rc_rep, ff.rc_icg, p.contact_cutoff, ff.mis});
+    for (auto &d : hsys) d.reach = (d.csl >= need_cut) ? 1 : 2;
+    build_tiles();
     nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
 
     hxyz.assign((size_t)3 * nb, 0.0f);
@@ -270,6 +266,19 @@ struct Engine {
     CK(cudaStreamSynchronize(stream));
   }
 
+  void build_tiles() {
+    htiles.clear();
+    for (int s = 0; s < (int)hsys.size(); ++s)
+      for (int b = 0; b < hsys[s].n; b += tile) htiles.push_back(Tile{s, hsys[s].bead_off + b});
+    hctiles.clear();
+    for (int s = 0; s < (int)hsys.size(); ++s) {
+      const int cps = hsys[s].cps;
+      for (int row = 0; row < cps * cps; ++row)
+        for (int x = 0; x < cps; x += PAIR_WARPS)
+          hctiles.push_back(Tile{s, hsys[s].cell_off + row * cps + x});
+    }
+  }
+
   // -------------------------------------------------------------- uploads
   void set_chain_flags() {
     for (int i = 0; i < nb; ++i) hflags[i] = type_to_flags(hpt[i], par.preset);
@@ -299,7 +308,7 @@ struct Engine {
 
   void recount() {
     CK(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (size_t)nblk * SCAN_CHUNK, stream));
-    k_count<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, counts.p,
+    k_count<<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, counts.p,
                                                            rank.p, d_err.p);
     CK(cudaGetLastError());
     kcount += 1;
@@ -371,7 +380,7 @@ struct Engine {
   }
 
   void launch_scatter(const float4 *src) {
-    k_scatter<<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+    k_scatter<<<(unsigned)htiles.size(), tile, 0, stream>>>(
         d_tiles.p, d_sys.p, src, rank.p, start.p, sorted.p,
         par.pair_kernel >= 2 ? fs.p : nullptr, d_err.p);
     kcount += 1;
@@ -380,20 +389,17 @@ struct Engine {
   template <int MODE>
   void launch_pair() {
     if (par.pair_kernel == 0)
-      k_pair<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+      k_pair<MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                   start.p, fs.p);
     else if (par.pair_kernel == 3 && par.reach == 2)
-      k_pair_flat<MODE, 2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+      k_pair_flat<MODE, 2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                           sorted.p, start.p, fs.p);
     else if (par.pair_kernel == 3)
-      k_pair_flat<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+      k_pair_flat<MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                        sorted.p, start.p, fs.p);
-    else if (par.pair_kernel == 2 && par.reach == 2)
-      k_pair_half<MODE, 2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+    else if (par.pair_kernel == 2)  // each system's own stencil reach
+      k_pair_half<MODE, 0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                           sorted.p, start.p, fs.p);
-    else if (par.pair_kernel == 2)
-      k_pair_half<MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, ff,
-                                                                       sorted.p, start.p, fs.p);
     else
       k_pair_cells<MODE><<<(unsigned)hctiles.size(), PAIR_WARPS * 32, 0, stream>>>(
           d_ctiles.p, d_sys.p, ff, sorted.p, start.p, fs.p);
@@ -402,7 +408,7 @@ struct Engine {
 
   template <int STAGE, int MODE>
   void launch_update() {
-    k_update<STAGE, MODE><<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+    k_update<STAGE, MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(
         d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, start.p, counts.p,
         lbs_sorted.p, lbs_start.p, d_step.p, d_err.p);
     kcount += 1;
@@ -427,19 +433,15 @@ struct Engine {
 
   // Observables on the cell-ordered copy of pos (must be current).
   void launch_contacts_args(const ContactArgs &a) {
-    if (par.reach == 2)
-      k_contacts<2><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
-                                                                    start.p, a);
-    else
-      k_contacts<1><<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
-                                                                    start.p, a);
+    k_contacts<0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                  start.p, a);
     kcount += 1;
   }
 
   void launch_contacts() { launch_contacts_args(contact_args(true, true, false)); }
 
   void launch_observe() {
-    k_observe<<<(unsigned)htiles.size(), TILE, 0, stream>>>(d_tiles.p, d_sys.p, pos.p,
+    k_observe<<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, pos.p,
                                                              CCP_RCO / 2.0f, obs.p);
     kcount += 1;
   }
@@ -502,6 +504,134 @@ struct Engine {
     if (e != cudaSuccess) throw Error(ST_CUDA, std::string("cuda: ") + cudaGetErrorString(e));
     graphs[key] = ge;
     return ge;
+  }
+
+  // Rebuilds the cell grids with per-system cell sides and the per-bead tile
+  // size; the state stays on the device and only the cell arrays change.
+  void regrid(const std::vector<float> &csl, int new_tile) {
+    CK(cudaStreamSynchronize(stream));
+    for (auto &g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
+    graph_kernels.clear();
+    tile = new_tile;
+    nc = 0;
+    for (size_t s = 0; s < hsys.size(); ++s) {
+      SysDesc &d = hsys[s];
+      d.csl = csl[s];
+      d.inv_csl = 1.0f / csl[s];
+      d.cps = std::max(2, 2 * (int)std::ceil(geo[s].d_m / csl[s]));
+      d.cell_off = nc;
+      d.reach = (csl[s] >= need_cut) ? 1 : 2;
+      nc += d.cps * d.cps * d.cps;
+    }
+    build_tiles();
+    nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    size_t cpad = (size_t)nblk * SCAN_CHUNK;
+    counts.alloc(cpad);
+    start.alloc(cpad + 4);
+    bsum.alloc(nblk + 1);
+    lbs_start.alloc(nc + 1);
+    d_tiles.alloc(htiles.size());
+    d_ctiles.alloc(hctiles.size());
+    CK(cudaMemcpyAsync(d_tiles.p, htiles.data(), sizeof(Tile) * htiles.size(),
+                       cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_ctiles.p, hctiles.data(), sizeof(Tile) * hctiles.size(),
+                       cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(start.p, 0, sizeof(uint32_t) * (cpad + 4), stream));
+    upload_lbs();  // re-sorts the sites into the new cells and uploads hsys
+    recount();
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  // Device ms per Heun step with the current grids (graphs of `reps` steps).
+  double time_steps(int reps) {
+    run_steps(reps, MODE_DST, 0);  // builds the graph
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, stream));
+    run_steps(reps, MODE_DST, 0);
+    CK(cudaEventRecord(e1, stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sync_and_check();
+    return ms / reps;
+  }
+
+  // Autotuner: per size class (bead counts in [2^k, 2^(k+1))) the cell side
+  // factor f (cell side = f * largest cutoff; f >= 1 uses the 3x3x3 stencil,
+  // f in [0.5, 1) the 5x5x5 one), then the per-bead tile size. Each candidate
+  // is timed over `reps` steps; the state, time and noise counter are restored
+  // afterwards, so tuning does not change the trajectory. Returns a JSON report.
+  std::string autotune(int reps) {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    if (par.pair_kernel != 2) throw Error(ST_ARG, "autotune needs the half-shell pair kernel");
+    download_positions();
+    std::vector<float> saved_xyz = hxyz;
+    uint64_t saved_step = step;
+    const int ns = (int)hsys.size();
+    std::vector<int> cls(ns);
+    std::map<int, std::vector<int>> members;
+    for (int s = 0; s < ns; ++s) {
+      int k = 0;
+      while ((2 << k) <= hsys[s].n) ++k;
+      cls[s] = k;
+      members[k].push_back(s);
+    }
+    std::vector<float> csl(ns);
+    for (int s = 0; s < ns; ++s) csl[s] = hsys[s].csl;
+    const float factors[] = {1.0f, 0.5f, 0.55f, 0.625f, 0.75f};
+    std::ostringstream rep;
+    rep << "{\"classes\": [";
+    bool first = true;
+    for (auto &kv : members) {
+      double best = 1e30;
+      float best_f = 1.0f;
+      std::ostringstream tried;
+      for (float f : factors) {
+        for (int s : kv.second) csl[s] = f * need_cut;
+        regrid(csl, tile);
+        double ms = time_steps(reps);
+        tried << (tried.tellp() > 0 ? ", " : "") << "[" << f << ", " << ms << "]";
+        if (ms < best) {
+          best = ms;
+          best_f = f;
+        }
+      }
+      for (int s : kv.second) csl[s] = best_f * need_cut;
+      int nmin = 1 << 30, nmax = 0;
+      for (int s : kv.second) {
+        nmin = std::min(nmin, hsys[s].n);
+        nmax = std::max(nmax, hsys[s].n);
+      }
+      rep << (first ? "" : ", ") << "{\"n_min\": " << nmin << ", \"n_max\": " << nmax
+          << ", \"systems\": " << kv.second.size() << ", \"cell_side\": " << best_f * need_cut
+          << ", \"reach\": " << (best_f >= 1.0f ? 1 : 2) << ", \"tried\": [" << tried.str()
+          << "]}";
+      first = false;
+    }
+    double best = 1e30;
+    int best_tile = tile;
+    std::ostringstream tt;
+    for (int t : {64, 128, 256}) {
+      regrid(csl, t);
+      double ms = time_steps(reps);
+      tt << (tt.tellp() > 0 ? ", " : "") << "[" << t << ", " << ms << "]";
+      if (ms < best) {
+        best = ms;
+        best_tile = t;
+      }
+    }
+    regrid(csl, best_tile);
+    hxyz = saved_xyz;
+    upload_positions();
+    step = saved_step;
+    rep << "], \"tile\": " << best_tile << ", \"tiles_tried\": [" << tt.str()
+        << "], \"ms_per_step\": " << best << "}";
+    return rep.str();
   }
 
   // Per-kernel device times of `reps` observed steps, each kernel bracketed by
@@ -642,7 +772,7 @@ struct Engine {
     if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
     sort_now();
     launch_pair<MODE_DST>();
-    k_total_force<MODE_DST><<<(unsigned)htiles.size(), TILE, 0, stream>>>(
+    k_total_force<MODE_DST><<<(unsigned)htiles.size(), tile, 0, stream>>>(
         d_tiles.p, d_sys.p, ff, pos.p, fs.p, rank.p, start.p, lbs_sorted.p, lbs_start.p, fout.p);
     recount();
     CK(cudaGetLastError());
@@ -964,6 +1094,16 @@ int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n) {
     need(n >= 7, "buffer too small");
     h->e->kernel_times(reps, out);
   });
+}
+
+int ccpgpu_autotune(ccpgpu_sim *h, int32_t reps, char *report, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h && reps > 0, "null argument");
+    std::string r = h->e->autotune(reps);
+    rc = put_bytes(r + std::string(1, '\0'), report, cap, len);
+  });
+  return g ? g : rc;
 }
 
 int ccpgpu_kernel_count(const ccpgpu_sim *h, uint64_t *count) {

@@ -461,7 +461,7 @@ __device__ __forceinline__ void pair_accum(float4 p, uint32_t wi, float4 q, cons
 // x-adjacent cells form one contiguous range of the sorted array. Pairs with
 // |i - j| <= 1 are skipped, also across chain ends (chrsim.cu:250).
 template <int MODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_pair(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
            const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
            float4 *__restrict__ fs) {
@@ -530,9 +530,10 @@ __device__ __forceinline__ void half_pair(float4 p, uint32_t wi, const float4 *_
 // REACH = 1: cells of side >= the largest cutoff, 3x3x3 neighbourhood.
 // REACH = 2: cells of side >= half of it, 5x5x5 neighbourhood: the candidate
 // volume drops from 27 to 15.6 cutoff-cubes (x0.58) at the price of 13 instead
-// of 5 row ranges per bead.
+// of 5 row ranges per bead. REACH = 0: each system's own reach (SysDesc), so
+// one launch serves systems gridded differently by the autotuner.
 template <int MODE, int REACH = 1>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_pair_half(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                 float4 *__restrict__ fs) {
@@ -540,12 +541,13 @@ __global__ void __launch_bounds__(128)
   const SysDesc &s = sys[t.sys];
   int slot = t.begin + threadIdx.x;
   if (slot >= s.bead_off + s.n) return;
+  const int R = (REACH > 0) ? REACH : s.reach;
   float4 p = sorted[slot];
   uint32_t wi = wbits(p);
   bool esc = false;
   CellXYZ c = cell_of(p, s, esc);
   const int cps = s.cps;
-  const int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
+  const int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
   float3 acc = make_float3(0.0f, 0.0f, 0.0f);
   // own cell after i, then the +x cells
   {
@@ -554,17 +556,17 @@ __global__ void __launch_bounds__(128)
     for (uint32_t k = slot + 1; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
   }
   // the +y rows of this layer, then all rows of the +z layers
-  constexpr int NR = REACH + REACH * (2 * REACH + 1);
+  const int NR = R + R * (2 * R + 1);
 #pragma unroll 1
   for (int r = 0; r < NR; ++r) {
     int y, z;
-    if (r < REACH) {
+    if (r < R) {
       y = c.y + 1 + r;
       z = c.z;
     } else {
-      int q = r - REACH;
-      y = c.y - REACH + q % (2 * REACH + 1);
-      z = c.z + 1 + q / (2 * REACH + 1);
+      int q = r - R;
+      y = c.y - R + q % (2 * R + 1);
+      z = c.z + 1 + q / (2 * R + 1);
     }
     if (y < 0 || y >= cps || z >= cps) continue;
     int row = s.cell_off + (z * cps + y) * cps;
@@ -599,7 +601,7 @@ __device__ __forceinline__ void half_row(const SysDesc &s, CellXYZ c, int r, int
 }
 
 template <int MODE, int REACH = 1>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_pair_flat(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                 float4 *__restrict__ fs) {
@@ -834,7 +836,7 @@ __device__ __forceinline__ void cap_step(float3 &D, float max_step) {
 // F = bonded + wall + LBS + pair (pair read from the cell-ordered result).
 // The written position is binned into the next counting sort.
 template <int STAGE, int MODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_update(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
              float4 *__restrict__ pos, float4 *__restrict__ er, float4 *__restrict__ fbuf,
              const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
@@ -986,7 +988,7 @@ struct ContactArgs {
 // the overlap count of the initial-condition relaxation (chrsim.cu:805-820).
 // REACH as for the pair kernel (cells of side >= cutoff / REACH).
 template <int REACH = 1>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_contacts(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
                const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                ContactArgs a) {
@@ -1006,9 +1008,10 @@ __global__ void __launch_bounds__(128)
     bool esc = false;
     CellXYZ c = cell_of(p, s, esc);
     const int cps = s.cps;
-    int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
-    for (int z = max(c.z - REACH, 0); z <= min(c.z + REACH, cps - 1); ++z)
-      for (int y = max(c.y - REACH, 0); y <= min(c.y + REACH, cps - 1); ++y) {
+    const int R = (REACH > 0) ? REACH : s.reach;  // 0: the system's own reach
+    int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+    for (int z = max(c.z - R, 0); z <= min(c.z + R, cps - 1); ++z)
+      for (int y = max(c.y - R, 0); y <= min(c.y + R, cps - 1); ++y) {
         int row = s.cell_off + (z * cps + y) * cps;
         uint32_t b = start[row + x0], e = start[row + x1 + 1];
         for (uint32_t k = b; k < e; ++k) {
@@ -1057,7 +1060,7 @@ constexpr int OBS_STRIDE = 4 + 3 * N_SHELLS;
 // to ~20 thin outer shells); the position sums for Rg^2 are reduced in FP64 by
 // warp shuffles. The CTA then folds the warp histograms into FP64 and adds the
 // non-zero entries to the system's accumulators.
-constexpr int OBS_WARPS = 4;
+constexpr int OBS_WARPS = 8;  // most warps of a CTA (tiles of up to 256 beads)
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -1131,7 +1134,8 @@ __global__ void __launch_bounds__(OBS_WARPS * 32)
   for (int k = threadIdx.x; k < 3 * N_SHELLS; k += blockDim.x) {
     double v = 0.0;
 #pragma unroll
-    for (int w = 0; w < OBS_WARPS; ++w) v += (double)hist[w][k];
+    for (int w = 0; w < OBS_WARPS; ++w)
+      if (w < (int)(blockDim.x >> 5)) v += (double)hist[w][k];
     if (v != 0.0) atomicAdd(&dst[4 + k], v);
   }
 }
@@ -1141,7 +1145,7 @@ __global__ void __launch_bounds__(OBS_WARPS * 32)
 // of p, FP32 distances accumulated in FP64.
 constexpr int SDIST_PCHUNK = 256;
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_sdist(const float4 *__restrict__ pos, const int32_t *__restrict__ chain_first,
             const int32_t *__restrict__ chain_len, const int32_t *__restrict__ chain_ps_off,
             const int32_t *__restrict__ chain_smax, int chain, double *__restrict__ ds) {
