@@ -397,7 +397,13 @@ struct Engine {
     else if (par.pair_kernel == 3)
       k_pair_flat<MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                        sorted.p, start.p, fs.p);
-    else if (par.pair_kernel == 2)  // each system's own stencil reach
+    else if (par.pair_kernel == 2 && uniform_reach() == 2)
+      k_pair_half<MODE, 2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                          sorted.p, start.p, fs.p);
+    else if (par.pair_kernel == 2 && uniform_reach() == 1)
+      k_pair_half<MODE, 1><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
+                                                                          sorted.p, start.p, fs.p);
+    else if (par.pair_kernel == 2)  // mixed: each system's own stencil reach
       k_pair_half<MODE, 0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                           sorted.p, start.p, fs.p);
     else
@@ -432,9 +438,25 @@ struct Engine {
   }
 
   // Observables on the cell-ordered copy of pos (must be current).
+  // 1 or 2 when every system uses that stencil reach, 0 when they differ
+  int uniform_reach() const {
+    int r = hsys.empty() ? 1 : hsys[0].reach;
+    for (const auto &d : hsys)
+      if (d.reach != r) return 0;
+    return r;
+  }
+
   void launch_contacts_args(const ContactArgs &a) {
-    k_contacts<0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
-                                                                  start.p, a);
+    const int r = uniform_reach();
+    if (r == 1)
+      k_contacts<1><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                    start.p, a);
+    else if (r == 2)
+      k_contacts<2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                    start.p, a);
+    else
+      k_contacts<0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+                                                                    start.p, a);
     kcount += 1;
   }
 
