@@ -1,7 +1,7 @@
 """Builds libccpgpu.so (the engine's C-ABI library) in-tree for sm_103a.
 
-Two translation units (host C++ and the CUDA engine) are compiled in
-parallel with nvcc and linked into tfm_gb300/libccpgpu.so. No cmake.
+Three translation units (host C++, the CUDA engine and the surrogate
+network) are compiled in parallel with nvcc and linked into tfm_gb300/libccpgpu.so. No cmake.
 """
 import os
 import shutil
@@ -31,7 +31,7 @@ def _run(cmd):
 
 
 def sources():
-    return [os.path.join(CSRC, f) for f in ("host.cpp", "engine.cu")]
+    return [os.path.join(CSRC, f) for f in ("host.cpp", "engine.cu", "surrogate.cu")]
 
 
 def _stale(target, deps):
@@ -43,7 +43,8 @@ def _stale(target, deps):
 
 def build(force=False, verbose=False):
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps.append(os.path.join(os.path.dirname(HERE), "include", "ccpgpu.h"))
+    for hdr in ("ccpgpu.h", "ccpgpu_surrogate.h"):
+        deps.append(os.path.join(os.path.dirname(HERE), "include", hdr))
     if not force and not _stale(OUT, deps):
         return OUT
     os.makedirs(OBJ, exist_ok=True)

@@ -918,6 +918,8 @@ struct ccpgpu_sim {
 
 static thread_local std::string g_last_error;
 
+void ccpgpu::set_last_error(const std::string &m) { g_last_error = m; }
+
 template <typename F>
 static int guarded(F &&f) {
   try {

@@ -83,6 +83,10 @@ struct Params {
 // chrsim.cu:421-435). Throws Error(ST_PARAM, ccp's message).
 Params parse_params(const std::string &text);
 
+// The calling thread's message for ccpgpu_last_error() (shared by every
+// entry point of the library).
+void set_last_error(const std::string &m);
+
 // Force field of a preset with its default temperature and time step (ccp:
 // T = 298 K, dt = 1/2048; baseline: kT = 1, dt = 1e-3); allocates nothing.
 ForceField make_preset(int preset);

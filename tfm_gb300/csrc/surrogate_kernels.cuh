@@ -1,0 +1,748 @@
+// Kernels of the contact-map surrogate network.
+//
+// Tensor-core kernels (tcgen05, TMA, TMEM):
+//  * k_conv_tc: implicit-GEMM convolution over channels-last BF16 images
+//    [B][H][W][C]. One CTA tile is 128 consecutive output pixels of one image
+//    row (M = 128) times all output channels (N = 64 or 128); K runs over
+//    taps x 64-channel input blocks. The A operand of each K block is one TMA
+//    load of the input tile shifted by the tap offset (out-of-image pixels
+//    arrive as zeros, which is the convolution's zero padding); the weights of
+//    all taps stay resident in shared memory. Accumulators live in TMEM,
+//    double-buffered so the epilogue of one tile overlaps the MMAs of the next.
+//    The epilogue fuses bias, ReLU, the residual add, the ReLU mask bits and
+//    the gradient masking of the backward pass. The same kernel computes the
+//    input gradient of a convolution with negated tap offsets and transposed
+//    weights.
+//  * k_wgrad_tc: weight (and bias) gradients. D[(tap, ci)][co] = sum over
+//    pixels p of X[p + tap offset][ci] dY[p][co] is a GEMM whose K dimension
+//    is the pixel; both operands come from channels-last tiles, so they are
+//    MN-major. Two (tap, channel block) "atoms" of 64 rows stack into M = 128;
+//    an all-ones atom gives the bias gradient. Each CTA reduces a range of
+//    pixels into FP32 partial sums that k_wgrad_reduce adds up in a fixed
+//    order.
+// CUDA-core kernels: sequence embedding, pooling, the outer-product pair
+// features and their gradient, the output layer with the loss, AdamW.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "tc.cuh"
+
+namespace sur {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int MAX_TAPS = 9;
+constexpr int CONV_THREADS = 192;  // warp 0: TMA, warp 1: MMA + TMEM, warps 2-5: epilogue
+constexpr int MAX_STAGES = 4;
+constexpr uint32_t A_TILE = 128u * 128u;  // 128 pixels x 64 BF16 channels
+constexpr uint32_t TMEM_COLS_CONV = 256;  // two accumulators of up to 128 columns
+
+struct ConvShape {
+  int B, H, W;     // image (input = output size); W is a multiple of 128
+  int cin_blocks;  // input channels / 64
+  int N;           // output channels: 64 or 128
+  int ntaps;
+  int stages;      // A-operand pipeline depth (2..4)
+  int n_tiles;     // B * H * W / 128
+  int dh[MAX_TAPS], dw[MAX_TAPS];  // input offset of each tap (row, column)
+};
+
+// Fused epilogue of k_conv_tc; every pointer is optional. Per output value:
+// v = acc + bias; mask bit = v > 0; v = relu(v); v += resid (BF16 or FP32);
+// out_f32 = v; out = v, zeroed where the bit of mask_in is clear.
+struct ConvEpi {
+  const float *bias;        // [N]
+  int relu;
+  const bf16 *resid;        // [P][N]
+  const float *resid_f32;   // [P][N]
+  float *out_f32;           // [P][N]
+  const uint32_t *mask_in;  // [P][N / 32]
+  bf16 *out;                // [P][N]
+  uint32_t *mask_out;       // [P][N / 32]
+};
+
+__host__ __device__ constexpr uint32_t conv_smem_bytes(int ntaps, int cin_blocks, int N, int stages) {
+  return 1024u + (uint32_t)(ntaps * cin_blocks) * (uint32_t)N * 128u + (uint32_t)stages * A_TILE + 256u;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+__device__ __forceinline__ void load_bf16x16(const bf16 *src, float *v) {
+  const uint4 *s = reinterpret_cast<const uint4 *>(src);
+  uint4 a = s[0], b = s[1];
+  uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    v[2 * i] = bf_lo(w[i]);
+    v[2 * i + 1] = bf_hi(w[i]);
+  }
+}
+
+__device__ __forceinline__ void store_bf16x16(bf16 *dst, const float *v) {
+  uint4 a, b;
+  a.x = pack_bf16(v[0], v[1]);
+  a.y = pack_bf16(v[2], v[3]);
+  a.z = pack_bf16(v[4], v[5]);
+  a.w = pack_bf16(v[6], v[7]);
+  b.x = pack_bf16(v[8], v[9]);
+  b.y = pack_bf16(v[10], v[11]);
+  b.z = pack_bf16(v[12], v[13]);
+  b.w = pack_bf16(v[14], v[15]);
+  uint4 *d = reinterpret_cast<uint4 *>(dst);
+  d[0] = a;
+  d[1] = b;
+}
+
+__device__ __forceinline__ void conv_epilogue16(const ConvEpi &e, size_t p, int N, int c0, float *v,
+                                                uint32_t &mask_lo) {
+  const size_t o = p * (size_t)N + c0;
+  if (e.bias) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] += __ldg(e.bias + c0 + i);
+  }
+  if (e.mask_out) {
+    uint32_t bits = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) bits |= (v[i] > 0.0f ? 1u : 0u) << i;
+    if ((c0 & 16) == 0)
+      mask_lo = bits;
+    else
+      e.mask_out[p * (size_t)(N >> 5) + (c0 >> 5)] = mask_lo | (bits << 16);
+  }
+  if (e.relu) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
+  }
+  if (e.resid) {
+    float r[16];
+    load_bf16x16(e.resid + o, r);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] += r[i];
+  }
+  if (e.resid_f32) {
+    const float4 *r = reinterpret_cast<const float4 *>(e.resid_f32 + o);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float4 x = r[i];
+      v[4 * i] += x.x;
+      v[4 * i + 1] += x.y;
+      v[4 * i + 2] += x.z;
+      v[4 * i + 3] += x.w;
+    }
+  }
+  if (e.out_f32) {
+    float4 *d = reinterpret_cast<float4 *>(e.out_f32 + o);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  }
+  if (e.mask_in) {
+    const uint32_t w = e.mask_in[p * (size_t)(N >> 5) + (c0 >> 5)] >> (c0 & 16);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = ((w >> i) & 1u) ? v[i] : 0.0f;
+  }
+  if (e.out) store_bf16x16(e.out + o, v);
+}
+
+// Implicit-GEMM convolution (see the file comment). tmx: 4-D map over the
+// input image {C, W, H, B} with box {64, 128, 1, 1}; tmw: 2-D map over the
+// weights {C_in, taps x N} with box {64, N}, both with 128-byte swizzle.
+// Grid: persistent, at most one CTA per SM; tiles strided by gridDim.x.
+__global__ void __launch_bounds__(CONV_THREADS, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
+              const ConvShape sh, const ConvEpi epi, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  const int nkb = sh.ntaps * sh.cin_blocks;
+  const int S = sh.stages;
+  const int N = sh.N;
+  const uint32_t w_tile = (uint32_t)N * 128u;
+  const uint32_t w_base = base;
+  const uint32_t a_base = w_base + (uint32_t)nkb * w_tile;
+  const uint32_t bar0 = a_base + (uint32_t)S * A_TILE;
+  // barriers: full[S], empty[S], tfull[2], tempty[2], weights, fin
+  const uint32_t full0 = bar0, empty0 = bar0 + 8u * S, tfull0 = bar0 + 16u * S,
+                 tempty0 = tfull0 + 16u, wbar = tempty0 + 16u, fin = wbar + 8u;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem_raw + (fin + 8u - raw));
+  volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      tc::mbar_init(full0 + 8u * s, 1);
+      tc::mbar_init(empty0 + 8u * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(tfull0 + 8u * b, 1);
+      tc::mbar_init(tempty0 + 8u * b, 4);
+    }
+    tc::mbar_init(wbar, 1);
+    tc::mbar_init(fin, 1);
+    *abort = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), TMEM_COLS_CONV);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const int wtiles = sh.W >> 7;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer: resident weights once, then one A tile per K block
+      tc::prefetch_map(&tmx);
+      tc::prefetch_map(&tmw);
+      tc::mbar_arrive_expect_tx(wbar, (uint32_t)nkb * w_tile);
+      for (int t = 0; t < sh.ntaps; ++t)
+        for (int cb = 0; cb < sh.cin_blocks; ++cb)
+          tc::tma_load_2d(w_base + (uint32_t)(t * sh.cin_blocks + cb) * w_tile, &tmw, wbar, cb * 64,
+                          t * N);
+      uint32_t it = 0;
+      for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x) {
+        const int wb = tile % wtiles, bh = tile / wtiles;
+        const int h = bh % sh.H, b = bh / sh.H;
+        for (int t = 0; t < sh.ntaps; ++t)
+          for (int cb = 0; cb < sh.cin_blocks; ++cb) {
+            const int s = (int)(it % (uint32_t)S);
+            const uint32_t r = it / (uint32_t)S;
+            if (!tc::mbar_wait(empty0 + 8u * s, (r & 1u) ^ 1u, abort)) goto produced;
+            tc::mbar_arrive_expect_tx(full0 + 8u * s, A_TILE);
+            tc::tma_load_4d(a_base + (uint32_t)s * A_TILE, &tmx, full0 + 8u * s, cb * 64,
+                            wb * 128 + sh.dw[t], h + sh.dh[t], b);
+            ++it;
+          }
+      }
+    produced:
+      // nothing may still be landing in shared memory when the CTA exits
+      tc::mbar_drain(wbar, 0);
+      for (uint32_t k = (it > (uint32_t)S ? it - (uint32_t)S : 0u); k < it; ++k)
+        tc::mbar_drain(full0 + 8u * (k % (uint32_t)S), (k / (uint32_t)S) & 1u);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      const uint32_t idesc = tc::idesc_bf16(128, N, false, false);
+      uint32_t it = 0;
+      int local = 0;
+      if (tc::mbar_wait(wbar, 0, abort)) {
+        for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
+          const int buf = local & 1;
+          const uint32_t use = (uint32_t)local >> 1;
+          if (!tc::mbar_wait(tempty0 + 8u * buf, (use & 1u) ^ 1u, abort)) break;
+          tc::fence_after_sync();
+          const uint32_t d = tmem + (uint32_t)(buf * N);
+          bool ok = true;
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            const int s = (int)(it % (uint32_t)S);
+            const uint32_t r = it / (uint32_t)S;
+            if (!tc::mbar_wait(full0 + 8u * s, r & 1u, abort)) {
+              ok = false;
+              break;
+            }
+            tc::fence_after_sync();
+            const uint32_t a0 = a_base + (uint32_t)s * A_TILE;
+            const uint32_t b0 = w_base + (uint32_t)kb * w_tile;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              tc::mma_bf16(d, tc::sdesc(a0 + 32u * k, 16u, 1024u), tc::sdesc(b0 + 32u * k, 16u, 1024u),
+                           idesc, (kb | k) != 0 ? 1u : 0u);
+            tc::mma_commit(empty0 + 8u * s);
+          }
+          if (!ok) break;
+          tc::mma_commit(tfull0 + 8u * buf);
+        }
+      }
+      tc::mma_commit(fin);
+      tc::mbar_drain(fin, 0);
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    int local = 0;
+    for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
+      const int buf = local & 1;
+      const uint32_t use = (uint32_t)local >> 1;
+      if (!tc::mbar_wait(tfull0 + 8u * buf, use & 1u, abort)) break;
+      tc::fence_after_sync();
+      const int wb = tile % wtiles, bh = tile / wtiles;
+      const size_t p = (size_t)bh * sh.W + (size_t)wb * 128 + row;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N);
+      uint32_t mask_lo = 0;
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(taddr + (uint32_t)c0, v);
+        conv_epilogue16(epi, p, N, c0, v, mask_lo);
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tempty0 + 8u * buf);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, TMEM_COLS_CONV);
+  }
+  if (threadIdx.x == 0 && *abort) atomicOr(err, 1);
+}
+
+// ------------------------------------------------------------------ weight gradients
+
+constexpr int MAX_ATOMS = 20;
+constexpr int WG_THREADS = 192;
+constexpr int WG_STAGES = 2;
+constexpr uint32_t WG_TILE = 64u * 128u;  // 64 pixels x 64 BF16 channels
+
+struct WgradShape {
+  int B, H, W;          // image; W is a multiple of 64
+  int N;                // dY channels (output channels of the layer): 64 or 128
+  int n_atoms;          // even; X atoms first, then all-ones atoms
+  int n_x;              // X atoms: (tap, input channel block), tap-major
+  int jobs_per_group;   // atom pairs per CTA (grid.y = groups)
+  int tmem_cols;        // power of two >= jobs_per_group * N
+  int kb_total;         // B * H * W / 64
+  int kb_per_cta;
+  int dh[MAX_ATOMS], dw[MAX_ATOMS], cb[MAX_ATOMS];
+};
+
+__host__ __device__ constexpr uint32_t wgrad_smem_bytes(int N, int jobs_per_group) {
+  return 1024u + (uint32_t)WG_STAGES * (uint32_t)(N / 64 + 2 * jobs_per_group) * WG_TILE + 2u * WG_TILE +
+         256u;
+}
+
+// Partial sums: partial[blockIdx.x][atom][co][row of the atom (input channel)].
+// tmx: map over X {C_in, W, H, B}, tmy: map over dY {N, W, H, B}, both with
+// box {64, 64, 1, 1} and 128-byte swizzle.
+__global__ void __launch_bounds__(WG_THREADS, 1)
+    k_wgrad_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmy,
+               const WgradShape sh, float *__restrict__ partial, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  const int N = sh.N, ny = N / 64;
+  const int n_jobs = sh.n_atoms / 2;
+  const int j0 = blockIdx.y * sh.jobs_per_group;
+  const int j1 = min(j0 + sh.jobs_per_group, n_jobs);
+  const int a0 = 2 * j0, a1 = 2 * j1;
+  const int nxg = max(0, min(a1, sh.n_x) - a0);  // X atoms loaded by this CTA
+  const uint32_t stage_bytes = (uint32_t)(ny + 2 * sh.jobs_per_group) * WG_TILE;
+  const uint32_t ones_base = base + WG_STAGES * stage_bytes;
+  const uint32_t bar0 = ones_base + 2u * WG_TILE;
+  const uint32_t full0 = bar0, empty0 = bar0 + 8u * WG_STAGES, done = bar0 + 16u * WG_STAGES,
+                 fin = done + 8u;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem_raw + (fin + 8u - raw));
+  volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  auto atom_addr = [&](int a, int s) -> uint32_t {
+    return a < sh.n_x ? base + (uint32_t)s * stage_bytes + (uint32_t)(ny + a - a0) * WG_TILE
+                      : ones_base + (uint32_t)(a - sh.n_x) * WG_TILE;
+  };
+
+  const int kb_begin = blockIdx.x * sh.kb_per_cta;
+  const int kb_end = min(kb_begin + sh.kb_per_cta, sh.kb_total);
+  const int nkb = kb_end - kb_begin;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // all-ones tiles (BF16 1.0), written through the generic proxy
+  {
+    uint32_t *ones = reinterpret_cast<uint32_t *>(smem_raw + (ones_base - raw));
+    for (uint32_t k = threadIdx.x; k < 2u * WG_TILE / 4u; k += blockDim.x) ones[k] = 0x3F803F80u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < WG_STAGES; ++s) {
+      tc::mbar_init(full0 + 8u * s, 1);
+      tc::mbar_init(empty0 + 8u * s, 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::mbar_init(fin, 1);
+    *abort = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), (uint32_t)sh.tmem_cols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const int HW = sh.H * sh.W;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tc::prefetch_map(&tmx);
+      tc::prefetch_map(&tmy);
+      const uint32_t bytes = (uint32_t)(ny + nxg) * WG_TILE;
+      int i = 0;
+      for (; i < nkb; ++i) {
+        const int s = i % WG_STAGES;
+        const uint32_t r = (uint32_t)(i / WG_STAGES);
+        if (!tc::mbar_wait(empty0 + 8u * s, (r & 1u) ^ 1u, abort)) break;
+        const int px0 = (kb_begin + i) * 64;
+        const int b = px0 / HW, rem = px0 - b * HW;
+        const int h = rem / sh.W, w0 = rem - h * sh.W;
+        const uint32_t fb = full0 + 8u * s;
+        tc::mbar_arrive_expect_tx(fb, bytes);
+        const uint32_t sb = base + (uint32_t)s * stage_bytes;
+        for (int c = 0; c < ny; ++c) tc::tma_load_4d(sb + (uint32_t)c * WG_TILE, &tmy, fb, c * 64, w0, h, b);
+        for (int a = a0; a < a0 + nxg; ++a)
+          tc::tma_load_4d(sb + (uint32_t)(ny + a - a0) * WG_TILE, &tmx, fb, sh.cb[a] * 64, w0 + sh.dw[a],
+                          h + sh.dh[a], b);
+      }
+      for (int k = max(0, i - WG_STAGES); k < i; ++k)
+        tc::mbar_drain(full0 + 8u * (k % WG_STAGES), (uint32_t)(k / WG_STAGES) & 1u);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16(128, N, true, true);
+      bool ok = true;
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % WG_STAGES;
+        const uint32_t r = (uint32_t)(i / WG_STAGES);
+        if (!tc::mbar_wait(full0 + 8u * s, r & 1u, abort)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t yb = base + (uint32_t)s * stage_bytes;
+        for (int j = j0; j < j1; ++j) {
+          const uint32_t xa = atom_addr(2 * j, s), xb = atom_addr(2 * j + 1, s);
+          const uint32_t d = tmem + (uint32_t)((j - j0) * N);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            tc::mma_bf16(d, tc::sdesc(xa + 2048u * k, xb - xa, 1024u), tc::sdesc(yb + 2048u * k, WG_TILE, 1024u),
+                         idesc, (i | k) != 0 ? 1u : 0u);
+        }
+        tc::mma_commit(empty0 + 8u * s);
+      }
+      if (ok) tc::mma_commit(done);
+      tc::mma_commit(fin);
+      tc::mbar_drain(fin, 0);
+    }
+  } else {
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    if (nkb > 0 && tc::mbar_wait(done, 0, abort)) {
+      tc::fence_after_sync();
+      for (int j = j0; j < j1; ++j) {
+        const int atom = 2 * j + (row >> 6);
+        float *dst = partial + ((size_t)blockIdx.x * sh.n_atoms + atom) * (size_t)N * 64 + (row & 63);
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((j - j0) * N);
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dst[(size_t)(c0 + i) * 64] = v[i];
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, (uint32_t)sh.tmem_cols);
+  }
+  if (threadIdx.x == 0 && *abort) atomicOr(err, 2);
+}
+
+// dW[tap][co][ci] = sum over chunks of the X atoms' partials, in chunk order;
+// db[co] from the first all-ones atom. cin_blocks: input channel blocks
+// (X atom a = tap * cin_blocks + block).
+__global__ void k_wgrad_reduce(const float *__restrict__ partial, int chunks, int n_atoms, int n_x,
+                               int N, int cin_blocks, float *__restrict__ dw, float *__restrict__ db) {
+  const int cin = cin_blocks * 64;
+  const int total = n_x * N * 64;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < total) {
+    const int ci = k & 63, co = (k >> 6) % N, a = k / (64 * N);
+    float s = 0.0f;
+    for (int c = 0; c < chunks; ++c) s += partial[((size_t)c * n_atoms + a) * (size_t)N * 64 + (size_t)co * 64 + ci];
+    const int tap = a / cin_blocks, blk = a - tap * cin_blocks;
+    dw[((size_t)tap * N + co) * cin + blk * 64 + ci] = s;
+  } else if (db && k < total + N) {
+    const int co = k - total;
+    float s = 0.0f;
+    for (int c = 0; c < chunks; ++c) s += partial[((size_t)c * n_atoms + n_x) * (size_t)N * 64 + (size_t)co * 64];
+    db[co] = s;
+  }
+}
+
+// ------------------------------------------------------------------ CUDA-core kernels
+
+// Sequence -> channels-last input [n][L][64]: channel 0 = A bead, 1 = B bead,
+// 2 = LAD bead, the rest zero. idx (optional) selects dataset rows.
+__global__ void k_embed(const uint8_t *__restrict__ types, const uint8_t *__restrict__ lad,
+                        const int32_t *__restrict__ idx, int L, int n, bf16 *__restrict__ x0) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)n * L) return;
+  const int b = (int)(k / L), l = (int)(k - (long long)b * L);
+  const long long row = idx ? idx[b] : b;
+  const uint8_t t = types[row * L + l];
+  const uint8_t f = lad ? lad[row * L + l] : 0;
+  uint4 *d = reinterpret_cast<uint4 *>(x0 + k * 64);
+  uint4 z = make_uint4(0, 0, 0, 0);
+  uint4 first = z;
+  first.x = pack_bf16(t == 0 ? 1.0f : 0.0f, t == 1 ? 1.0f : 0.0f);
+  first.y = pack_bf16(f ? 1.0f : 0.0f, 0.0f);
+  d[0] = first;
+#pragma unroll
+  for (int i = 1; i < 8; ++i) d[i] = z;
+}
+
+// Mean over `f` consecutive positions: h [n][L][C] -> hp [n][L / f][C].
+__global__ void k_pool(const bf16 *__restrict__ h, int L, int C, int f, int n, bf16 *__restrict__ hp) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int M = L / f;
+  if (k >= (long long)n * M * C) return;
+  const int c = (int)(k % C);
+  const long long bm = k / C;
+  const long long src = bm * f * C + c;
+  float s = 0.0f;
+  for (int i = 0; i < f; ++i) s += __bfloat162float(h[src + (long long)i * C]);
+  hp[k] = __float2bfloat16_rn(s / (float)f);
+}
+
+// Pair features of the head input: z0[b][i][j][c] = u_i[c] v_j[c] + u_j[c] v_i[c]
+// + E[|i - j|][c], u = uv[..][0, 64), v = uv[..][64, 128). Block: one row i.
+__global__ void __launch_bounds__(256)
+    k_pair_fwd(const bf16 *__restrict__ uv, const float *__restrict__ E, int M, bf16 *__restrict__ z0) {
+  const int i = blockIdx.x, b = blockIdx.y;
+  __shared__ float ui[64], vi[64];
+  const bf16 *row = uv + ((size_t)b * M + i) * 128;
+  if (threadIdx.x < 64) {
+    ui[threadIdx.x] = __bfloat162float(row[threadIdx.x]);
+    vi[threadIdx.x] = __bfloat162float(row[64 + threadIdx.x]);
+  }
+  __syncthreads();
+  // thread -> (j, 16-channel chunk)
+  for (int k = threadIdx.x; k < M * 4; k += blockDim.x) {
+    const int j = k >> 2, c0 = (k & 3) * 16;
+    const bf16 *rj = uv + ((size_t)b * M + j) * 128;
+    float uj[16], vj[16], v[16];
+    load_bf16x16(rj + c0, uj);
+    load_bf16x16(rj + 64 + c0, vj);
+    const float *e = E + (size_t)abs(i - j) * 64 + c0;
+#pragma unroll
+    for (int t = 0; t < 16; ++t) v[t] = fmaf(ui[c0 + t], vj[t], fmaf(uj[t], vi[c0 + t], e[t]));
+    store_bf16x16(z0 + (((size_t)b * M + i) * M + j) * 64 + c0, v);
+  }
+}
+
+// Output layer: y[p] = wo . z[p] + bo over 64 channels; one thread per pixel.
+__global__ void k_head_out(const bf16 *__restrict__ z, const float *__restrict__ wo, const float *__restrict__ bo,
+                           long long P, float *__restrict__ y) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  float s = bo[0];
+  for (int c0 = 0; c0 < 64; c0 += 16) {
+    float v[16];
+    load_bf16x16(z + p * 64 + c0, v);
+#pragma unroll
+    for (int t = 0; t < 16; ++t) s = fmaf(__ldg(wo + c0 + t), v[t], s);
+  }
+  y[p] = s;
+}
+
+// Prediction: symmetrised log map -> contact probability max(exp(yhat) - eps, 0).
+__global__ void k_predict_maps(const float *__restrict__ y, int M, int n, float eps, float *__restrict__ out) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)n * M * M) return;
+  const long long b = k / ((long long)M * M);
+  const int r = (int)(k - b * M * M), i = r / M, j = r - i * M;
+  const float yh = 0.5f * (y[k] + y[b * M * M + (long long)j * M + i]);
+  out[k] = fmaxf(expf(yh) - eps, 0.0f);
+}
+
+// Loss and the gradient entering the head. yhat = (y + y^T) / 2, loss =
+// mean (yhat - t)^2 over n M^2 values (targets symmetric, so dL/dy = dL/dyhat).
+// Writes dz[p][c] = dy wo[c] (FP32), dc[p][c] = dz masked by the last head
+// layer's ReLU bits (BF16), and accumulates d wo, d bo and the loss.
+__global__ void __launch_bounds__(256)
+    k_loss_out_bwd(const float *__restrict__ y, const float *__restrict__ target, const int32_t *__restrict__ idx,
+                   const bf16 *__restrict__ z, const uint32_t *__restrict__ mask, const float *__restrict__ wo,
+                   int M, int n, float *__restrict__ dz, bf16 *__restrict__ dc, float *__restrict__ gwo,
+                   float *__restrict__ gbo, double *__restrict__ loss) {
+  __shared__ float swo[64];
+  __shared__ float red[8][65];
+  if (threadIdx.x < 64) swo[threadIdx.x] = wo[threadIdx.x];
+  __syncthreads();
+  const long long MM = (long long)M * M;
+  const long long P = (long long)n * MM;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float gw[64];
+#pragma unroll
+  for (int c = 0; c < 64; ++c) gw[c] = 0.0f;
+  float dyv = 0.0f, l2 = 0.0f;
+  if (p < P) {
+    const long long b = p / MM;
+    const int r = (int)(p - b * MM), i = r / M, j = r - i * M;
+    const float yh = 0.5f * (y[p] + y[b * MM + (long long)j * M + i]);
+    const long long row = idx ? idx[b] : b;
+    const float d = yh - target[row * MM + r];
+    l2 = d * d;
+    dyv = 2.0f * d / (float)P;
+    const uint32_t m0 = mask[p * 2], m1 = mask[p * 2 + 1];
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      float zv[16], g[16];
+      load_bf16x16(z + p * 64 + c0, zv);
+      const uint32_t w = (c0 < 32 ? m0 : m1) >> (c0 & 16);
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        g[t] = dyv * swo[c0 + t];
+        gw[c0 + t] = dyv * zv[t];
+      }
+      float4 *o = reinterpret_cast<float4 *>(dz + p * 64 + c0);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) o[t] = make_float4(g[4 * t], g[4 * t + 1], g[4 * t + 2], g[4 * t + 3]);
+#pragma unroll
+      for (int t = 0; t < 16; ++t) g[t] = ((w >> t) & 1u) ? g[t] : 0.0f;
+      store_bf16x16(dc + p * 64 + c0, g);
+    }
+  }
+  // block reduction of gw (64), dy (1) and loss (1)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < 64; ++c) {
+    float v = gw[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][c] = v;
+  }
+  float vdy = dyv, vl = l2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    vdy += __shfl_xor_sync(0xffffffffu, vdy, o);
+    vl += __shfl_xor_sync(0xffffffffu, vl, o);
+  }
+  __shared__ float rdy[8], rl[8];
+  if (lane == 0) {
+    rdy[warp] = vdy;
+    rl[warp] = vl;
+  }
+  __syncthreads();
+  if (threadIdx.x < 64) {
+    float s = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+    atomicAdd(gwo + threadIdx.x, s);
+  } else if (threadIdx.x == 64) {
+    float s = 0.0f, t = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      s += rdy[w];
+      t += rl[w];
+    }
+    atomicAdd(gbo, s);
+    atomicAdd(loss, (double)t / (double)P);
+  }
+}
+
+// Gradient of the pair features w.r.t. u and v: with S_ij = dz_ij + dz_ji,
+// du_i = sum_j S_ij v_j and dv_i = sum_j S_ij u_j (per channel). Block: row i
+// of sample b; 256 threads = 4 groups over j x 64 channels. Output BF16.
+__global__ void __launch_bounds__(256)
+    k_pair_bwd(const float *__restrict__ dz, const bf16 *__restrict__ uv, int M, bf16 *__restrict__ duv) {
+  const int i = blockIdx.x, b = blockIdx.y;
+  const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
+  const size_t MM = (size_t)M * M;
+  const float *dzb = dz + (size_t)b * MM * 64;
+  const bf16 *uvb = uv + (size_t)b * M * 128;
+  float du = 0.0f, dv = 0.0f;
+  for (int j = g; j < M; j += 4) {
+    const float s = dzb[((size_t)i * M + j) * 64 + c] + dzb[((size_t)j * M + i) * 64 + c];
+    du = fmaf(s, __bfloat162float(uvb[(size_t)j * 128 + 64 + c]), du);
+    dv = fmaf(s, __bfloat162float(uvb[(size_t)j * 128 + c]), dv);
+  }
+  __shared__ float su[4][64], sv[4][64];
+  su[g][c] = du;
+  sv[g][c] = dv;
+  __syncthreads();
+  if (g == 0) {
+    const float a = su[0][c] + su[1][c] + su[2][c] + su[3][c];
+    const float d = sv[0][c] + sv[1][c] + sv[2][c] + sv[3][c];
+    duv[((size_t)b * M + i) * 128 + c] = __float2bfloat16_rn(a);
+    duv[((size_t)b * M + i) * 128 + 64 + c] = __float2bfloat16_rn(d);
+  }
+}
+
+// Gradient of the distance embedding: dE[s][c] = sum over samples and over
+// pairs with |i - j| = s of dz_ij[c]. Block: one separation s; 64 channels x 4.
+__global__ void __launch_bounds__(256)
+    k_dist_bwd(const float *__restrict__ dz, int M, int n, float *__restrict__ dE) {
+  const int s = blockIdx.x;
+  const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
+  const size_t MM = (size_t)M * M;
+  float acc = 0.0f;
+  for (int b = 0; b < n; ++b) {
+    const float *dzb = dz + (size_t)b * MM * 64;
+    for (int i = g; i + s < M; i += 4) {
+      acc += dzb[((size_t)i * M + i + s) * 64 + c];
+      if (s) acc += dzb[((size_t)(i + s) * M + i) * 64 + c];
+    }
+  }
+  __shared__ float r[4][64];
+  r[g][c] = acc;
+  __syncthreads();
+  if (g == 0) dE[(size_t)s * 64 + c] = r[0][c] + r[1][c] + r[2][c] + r[3][c];
+}
+
+// Unpooling of the projection-input gradient: dz[b][l][c] = dhp[b][l / f][c] / f
+// (FP32, the encoder's residual gradient) and dc = dz masked by the last
+// encoder layer's ReLU bits (BF16). C = 128.
+__global__ void k_unpool(const float *__restrict__ dhp, const uint32_t *__restrict__ mask, int L, int f,
+                         int n, float *__restrict__ dz, bf16 *__restrict__ dc) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (b, l, 16-channel chunk)
+  if (k >= (long long)n * L * 8) return;
+  const int c0 = (int)(k & 7) * 16;
+  const long long bl = k >> 3;
+  const long long b = bl / L;
+  const int l = (int)(bl - b * L);
+  const float *src = dhp + ((b * (L / f)) + l / f) * 128 + c0;
+  const float inv = 1.0f / (float)f;
+  float v[16];
+#pragma unroll
+  for (int t = 0; t < 16; ++t) v[t] = src[t] * inv;
+  float4 *o = reinterpret_cast<float4 *>(dz + bl * 128 + c0);
+#pragma unroll
+  for (int t = 0; t < 4; ++t) o[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]);
+  const uint32_t w = mask[bl * 4 + (c0 >> 5)] >> (c0 & 16);
+#pragma unroll
+  for (int t = 0; t < 16; ++t) v[t] = ((w >> t) & 1u) ? v[t] : 0.0f;
+  store_bf16x16(dc + bl * 128 + c0, v);
+}
+
+// AdamW on one parameter segment (FP32 master weights).
+__global__ void k_adamw(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                        float *__restrict__ v, long long n, float lr, float b1, float b2, float eps,
+                        float wd, float bc1, float bc2) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float gk = g[k];
+  const float mk = b1 * m[k] + (1.0f - b1) * gk;
+  const float vk = b2 * v[k] + (1.0f - b2) * gk * gk;
+  m[k] = mk;
+  v[k] = vk;
+  const float upd = (mk / bc1) / (sqrtf(vk / bc2) + eps);
+  p[k] = p[k] * (1.0f - lr * wd) - lr * upd;
+}
+
+// BF16 copies of a convolution's weights: W [taps][co][ci] and the transposed
+// WT [taps][ci][co] used by the input-gradient convolution.
+__global__ void k_weights_bf16(const float *__restrict__ w, int taps, int co, int ci, bf16 *__restrict__ wb,
+                               bf16 *__restrict__ wt) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)taps * co * ci) return;
+  const int i = (int)(k % ci), o = (int)((k / ci) % co), t = (int)(k / ((long long)ci * co));
+  const bf16 x = __float2bfloat16_rn(w[k]);
+  wb[k] = x;
+  wt[((long long)t * ci + i) * co + o] = x;
+}
+
+}  // namespace sur
