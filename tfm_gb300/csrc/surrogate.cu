@@ -132,7 +132,6 @@ static const DevInfo &dev_info() {
   if (dev != dev_seen) {
     SCK(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
     SCK(cudaDeviceGetAttribute(&d.max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    SCK(cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, d.max_smem));
     SCK(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, d.max_smem));
     dev_seen = dev;
   }
@@ -152,31 +151,57 @@ struct Launcher {
   int *err = nullptr;
   long long kernels = 0;
 
-  // k_conv_tc over images of B x H x W pixels, cin -> N channels.
+  // k_conv_tc over images of B x H x W pixels, cin -> N channels. The taps
+  // must form an R x C grid with uniform steps (t = r C + c at ((r - R/2)
+  // step_h, (c - C/2) step_w)), R in {1, 3}, C in {1, 3, 5}.
   void conv(const CUtensorMap &x, const CUtensorMap &w, int B, int H, int W, int cin, int N, const Taps &taps,
             const ConvEpi &epi) {
     const DevInfo &d = dev_info();
-    if (W % 128 || cin % 64 || (N != 64 && N != 128) || taps.empty() || (int)taps.size() > MAX_TAPS)
-      throw Error(ST_ARG, "convolution shape not supported (W % 128, C in {64, 128}, <= 9 taps)");
+    if (W % 128 || (cin != 64 && cin != 128) || (N != 64 && N != 128))
+      throw Error(ST_ARG, "convolution shape not supported (W % 128, channels 64 or 128)");
+    const int nt = (int)taps.size();
+    int R, C;
+    if (nt == 9) R = 3, C = 3;
+    else if (nt == 5) R = 1, C = 5;
+    else if (nt == 3) R = 1, C = 3;
+    else if (nt == 1) R = 1, C = 1;
+    else throw Error(ST_ARG, "tap pattern not supported (3x3, 1x5, 1x3 or 1x1 grids)");
     ConvShape sh{};
     sh.B = B;
     sh.H = H;
     sh.W = W;
-    sh.cin_blocks = cin / 64;
-    sh.N = N;
-    sh.ntaps = (int)taps.size();
-    for (int t = 0; t < sh.ntaps; ++t) {
-      sh.dh[t] = taps[t].first;
-      sh.dw[t] = taps[t].second;
-    }
+    sh.step_h = R > 1 ? taps[(R - 1) * C].first / (R / 2) : 0;
+    sh.step_w = C > 1 ? taps[C - 1].second / (C / 2) : 0;
+    for (int t = 0; t < nt; ++t)
+      if (taps[t].first != (t / C - R / 2) * sh.step_h || taps[t].second != (t % C - C / 2) * sh.step_w)
+        throw Error(ST_ARG, "tap pattern not supported (3x3, 1x5, 1x3 or 1x1 grids)");
+    if (std::abs(sh.step_w) * (C / 2) > WIN_RADIUS) throw Error(ST_ARG, "tap column offset above the window radius");
+    const int cb = cin / 64;
     sh.stages = MAX_STAGES;
-    while (sh.stages > 2 && (int)conv_smem_bytes(sh.ntaps, sh.cin_blocks, N, sh.stages) > d.max_smem) --sh.stages;
-    const uint32_t smem = conv_smem_bytes(sh.ntaps, sh.cin_blocks, N, sh.stages);
+    while (sh.stages > 2 && (int)conv_smem_bytes(nt, cb, N, sh.stages) > d.max_smem) --sh.stages;
+    const uint32_t smem = conv_smem_bytes(nt, cb, N, sh.stages);
     if ((int)smem > d.max_smem) throw Error(ST_ARG, "convolution weights do not fit in shared memory");
     sh.n_tiles = B * H * (W / 128);
     if (sh.n_tiles == 0) return;
     const int grid = std::min(sh.n_tiles, d.sms);
-    k_conv_tc<<<grid, CONV_THREADS, smem, st>>>(x, w, sh, epi, err);
+    bool launched = false;
+#define SUR_CONV(N_, R_, C_, CB_)                                                              \
+  if (N == N_ && R == R_ && C == C_ && cb == CB_) {                                            \
+    static bool attr = false;                                                                  \
+    if (!attr) {                                                                               \
+      SCK(cudaFuncSetAttribute(k_conv_tc<N_, R_, C_, CB_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               d.max_smem));                                                   \
+      attr = true;                                                                             \
+    }                                                                                          \
+    k_conv_tc<N_, R_, C_, CB_><<<grid, CONV_THREADS, smem, st>>>(x, w, sh, epi, err);          \
+    launched = true;                                                                           \
+  }
+#define SUR_CONV_N(R_, C_, CB_) SUR_CONV(64, R_, C_, CB_) SUR_CONV(128, R_, C_, CB_)
+    SUR_CONV_N(3, 3, 1) SUR_CONV_N(3, 3, 2) SUR_CONV_N(1, 5, 1) SUR_CONV_N(1, 5, 2)
+    SUR_CONV_N(1, 3, 1) SUR_CONV_N(1, 3, 2) SUR_CONV_N(1, 1, 1) SUR_CONV_N(1, 1, 2)
+#undef SUR_CONV_N
+#undef SUR_CONV
+    if (!launched) throw Error(ST_ARG, "convolution configuration not instantiated");
     SCK(cudaGetLastError());
     ++kernels;
   }
@@ -239,8 +264,7 @@ struct Launcher {
     if ((size_t)chunks * sh.n_atoms * N * 64 > partial_cap) throw Error(ST_STATE, "partial-sum buffer too small");
     k_wgrad_tc<<<dim3(chunks, groups), WG_THREADS, smem, st>>>(x64, y64, sh, partial, err);
     SCK(cudaGetLastError());
-    const int total = sh.n_x * N * 64 + (db ? N : 0);
-    k_wgrad_reduce<<<(total + 255) / 256, 256, 0, st>>>(partial, chunks, sh.n_atoms, sh.n_x, N, cbs, dw, db);
+    k_wgrad_reduce<<<sh.n_x * N + (db ? N : 0), 256, 0, st>>>(partial, chunks, sh.n_atoms, sh.n_x, N, cbs, dw, db);
     SCK(cudaGetLastError());
     kernels += 2;
   }
@@ -299,7 +323,7 @@ static Config parse_config(const std::string &text) {
   if (c.head_width != 64) fail("head_width must be 64");
   if ((int)c.dilations.size() != c.head_layers) fail("dilations must list one value per head layer");
   for (int d : c.dilations)
-    if (d < 1 || d > c.bins / 2) fail("dilation out of range");
+    if (d < 1 || d > WIN_RADIUS) fail("dilation out of range");
   if (!(c.lr > 0) || !(c.target_eps > 0)) fail("lr and target_eps must be positive");
   return c;
 }
@@ -330,15 +354,16 @@ struct Net {
   Buf<bf16> x0, hp, uv;
   std::vector<Buf<bf16>> h, z;             // h[1..enc_layers], z[0..head_layers]
   std::vector<Buf<uint32_t>> emask, hmask;  // emask[1..], hmask[1..]
-  Buf<float> y, pred;
+  Buf<float> y, pred, dyb, dist_part;
+  Buf<uint8_t> decay;
   // backward
   Buf<float> hdz[2], edz[2], dhp;
   Buf<bf16> hdc[2], edc[2], duv;
   Buf<float> partial;
   Buf<double> loss;
   Buf<int> err;
-  // tensor maps: *128 for the convolution (box of 128 pixels), *64 for the
-  // weight gradient (box of 64 pixels)
+  // tensor maps: *128 for the convolution (box of WIN_ROWS pixels: a tile of
+  // 128 plus the tap margin), *64 for the weight gradient (box of 64 pixels)
   CUtensorMap m_x0_64{}, m_x0_128{}, m_hp_64{}, m_hp_128{}, m_duv_64{}, m_duv_128{};
   std::vector<CUtensorMap> m_h_64, m_h_128, m_z_64, m_z_128;
   CUtensorMap m_hdc_64[2]{}, m_hdc_128[2]{}, m_edc_64[2]{}, m_edc_128[2]{};
@@ -404,6 +429,14 @@ struct Net {
     adam_m.zero(st);
     adam_v.zero(st);
     init_params(seed);
+    {
+      std::vector<uint8_t> dflag(n_params, 0);
+      for (const Seg &sg : segs)
+        if (sg.decay) std::fill(dflag.begin() + sg.off, dflag.begin() + sg.off + sg.n, (uint8_t)1);
+      decay.alloc(n_params);
+      SCK(cudaMemcpyAsync(decay.p, dflag.data(), n_params, cudaMemcpyHostToDevice, st));
+      SCK(cudaStreamSynchronize(st));
+    }
     for (Layer *l : all_layers()) {
       l->wb.alloc((size_t)l->taps * l->cout * l->cin);
       l->wt.alloc((size_t)l->taps * l->cout * l->cin);
@@ -460,12 +493,22 @@ struct Net {
   }
 
   void refresh_weights() {
+    WeightTable t{};
+    long long most = 0;
     for (Layer *l : all_layers()) {
-      const long long n = (long long)l->taps * l->cout * l->cin;
-      k_weights_bf16<<<blocks(n), 256, 0, st>>>(params.p + l->w_off, l->taps, l->cout, l->cin, l->wb.p, l->wt.p);
-      SCK(cudaGetLastError());
-      ++run.kernels;
+      if (t.n == MAX_LAYERS) throw Error(ST_PARAM, "too many layers");
+      t.taps[t.n] = l->taps;
+      t.co[t.n] = l->cout;
+      t.ci[t.n] = l->cin;
+      t.off[t.n] = (long long)l->w_off;
+      t.wb[t.n] = l->wb.p;
+      t.wt[t.n] = l->wt.p;
+      most = std::max(most, (long long)l->taps * l->cout * l->cin);
+      ++t.n;
     }
+    k_weights_bf16<<<dim3(blocks(most), t.n), 256, 0, st>>>(params.p, t);
+    SCK(cudaGetLastError());
+    ++run.kernels;
   }
 
   void alloc_activations() {
@@ -473,7 +516,7 @@ struct Net {
     const size_t PL = (size_t)B * L, PM = (size_t)B * M, PMM = (size_t)B * M * M;
     x0.alloc(PL * 64);
     m_x0_64 = image_map(x0.p, 64, L, 1, B, 64);
-    m_x0_128 = image_map(x0.p, 64, L, 1, B, 128);
+    m_x0_128 = image_map(x0.p, 64, L, 1, B, WIN_ROWS);
     h.resize(cfg.enc_layers + 1);
     emask.resize(cfg.enc_layers + 1);
     m_h_64.resize(cfg.enc_layers + 1);
@@ -482,12 +525,12 @@ struct Net {
       h[l].alloc(PL * 128);
       emask[l].alloc(PL * 4);
       m_h_64[l] = image_map(h[l].p, 128, L, 1, B, 64);
-      m_h_128[l] = image_map(h[l].p, 128, L, 1, B, 128);
+      m_h_128[l] = image_map(h[l].p, 128, L, 1, B, WIN_ROWS);
     }
     hp.alloc(PM * 128);
     uv.alloc(PM * 128);
     m_hp_64 = image_map(hp.p, 128, M, 1, B, 64);
-    m_hp_128 = image_map(hp.p, 128, M, 1, B, 128);
+    m_hp_128 = image_map(hp.p, 128, M, 1, B, WIN_ROWS);
     z.resize(cfg.head_layers + 1);
     hmask.resize(cfg.head_layers + 1);
     m_z_64.resize(cfg.head_layers + 1);
@@ -495,24 +538,26 @@ struct Net {
     for (int l = 0; l <= cfg.head_layers; ++l) {
       z[l].alloc(PMM * 64);
       m_z_64[l] = image_map(z[l].p, 64, M, M, B, 64);
-      m_z_128[l] = image_map(z[l].p, 64, M, M, B, 128);
+      m_z_128[l] = image_map(z[l].p, 64, M, M, B, WIN_ROWS);
       if (l > 0) hmask[l].alloc(PMM * 2);
     }
     y.alloc(PMM);
     pred.alloc(PMM);
+    dyb.alloc(PMM);
+    dist_part.alloc((size_t)B * M * 64);
     for (int k = 0; k < 2; ++k) {
       hdz[k].alloc(PMM * 64);
       hdc[k].alloc(PMM * 64);
       m_hdc_64[k] = image_map(hdc[k].p, 64, M, M, B, 64);
-      m_hdc_128[k] = image_map(hdc[k].p, 64, M, M, B, 128);
+      m_hdc_128[k] = image_map(hdc[k].p, 64, M, M, B, WIN_ROWS);
       edz[k].alloc(PL * 128);
       edc[k].alloc(PL * 128);
       m_edc_64[k] = image_map(edc[k].p, 128, L, 1, B, 64);
-      m_edc_128[k] = image_map(edc[k].p, 128, L, 1, B, 128);
+      m_edc_128[k] = image_map(edc[k].p, 128, L, 1, B, WIN_ROWS);
     }
     duv.alloc(PM * 128);
     m_duv_64 = image_map(duv.p, 128, M, 1, B, 64);
-    m_duv_128 = image_map(duv.p, 128, M, 1, B, 128);
+    m_duv_128 = image_map(duv.p, 128, M, 1, B, WIN_ROWS);
     dhp.alloc(PM * 128);
     size_t pc = 0;
     pc = std::max(pc, Launcher::partial_floats(B, M, M, 64, 64, 9, true));
@@ -524,8 +569,9 @@ struct Net {
 
   // ---------------------------------------------------------------- passes
 
-  // Forward over n sequences (types/lad device arrays, rows optional) into y.
-  void forward(const uint8_t *types, const uint8_t *lad, const int32_t *rows, int n) {
+  // Forward over n sequences (types/lad device arrays, rows optional) into y;
+  // `training` keeps what the backward pass needs (ReLU masks, last output).
+  void forward(const uint8_t *types, const uint8_t *lad, const int32_t *rows, int n, bool training) {
     k_embed<<<blocks((long long)n * L), 256, 0, st>>>(types, lad, rows, L, n, x0.p);
     SCK(cudaGetLastError());
     ++run.kernels;
@@ -536,7 +582,7 @@ struct Net {
       e.relu = 1;
       e.resid = l > 0 ? h[l].p : nullptr;
       e.out = h[l + 1].p;
-      e.mask_out = emask[l + 1].p;
+      e.mask_out = training ? emask[l + 1].p : nullptr;
       run.conv(l == 0 ? m_x0_128 : m_h_128[l], ly.map_w, n, 1, L, ly.cin, 128, ly.off, e);
     }
     k_pool<<<blocks((long long)n * M * 128), 256, 0, st>>>(h[cfg.enc_layers].p, L, 128, f, n, hp.p);
@@ -548,23 +594,28 @@ struct Net {
       e.out = uv.p;
       run.conv(m_hp_128, proj.map_w, n, 1, M, 128, 128, proj.off, e);
     }
-    k_pair_fwd<<<dim3(M, n), 256, 0, st>>>(uv.p, params.p + E_off, M, z[0].p);
+    k_pair_fwd<<<dim3(M / PAIR_ROWS, n), 256, 0, st>>>(uv.p, params.p + E_off, M, z[0].p);
     SCK(cudaGetLastError());
     ++run.kernels;
+    const long long P = (long long)n * M * M;
+    SCK(cudaMemsetAsync(y.p, 0, sizeof(float) * P, st));
     for (int l = 0; l < cfg.head_layers; ++l) {
       const Layer &ly = head[l];
+      const bool last = l == cfg.head_layers - 1;
       ConvEpi e{};
       e.bias = params.p + ly.b_off;
       e.relu = 1;
       e.resid = z[l].p;
-      e.out = z[l + 1].p;
-      e.mask_out = hmask[l + 1].p;
+      // the last layer's output is needed only by the backward pass
+      e.out = (!last || training) ? z[l + 1].p : nullptr;
+      e.mask_out = training ? hmask[l + 1].p : nullptr;
+      if (last) {  // output layer fused into the epilogue
+        e.wo = params.p + wo_off;
+        e.bo = params.p + bo_off;
+        e.y = y.p;
+      }
       run.conv(m_z_128[l], ly.map_w, n, M, M, 64, 64, ly.off, e);
     }
-    const long long P = (long long)n * M * M;
-    k_head_out<<<blocks(P), 256, 0, st>>>(z[cfg.head_layers].p, params.p + wo_off, params.p + bo_off, P, y.p);
-    SCK(cudaGetLastError());
-    ++run.kernels;
   }
 
   // Backward of the loss on dataset rows (after forward on the same rows).
@@ -574,28 +625,38 @@ struct Net {
     const long long P = (long long)n * M * M;
     const int HL = cfg.head_layers;
     k_loss_out_bwd<<<blocks(P), 256, 0, st>>>(y.p, ds_target.p, rows, z[HL].p, hmask[HL].p, params.p + wo_off, M, n,
-                                              hdz[0].p, hdc[0].p, grads.p + wo_off, grads.p + bo_off, loss.p);
+                                              dyb.p, hdc[0].p, grads.p + wo_off, grads.p + bo_off, loss.p);
     SCK(cudaGetLastError());
     ++run.kernels;
-    int k = 0;
+    int kc = 0;   // dc_l is in hdc[kc]
+    int kz = -1;  // dz_{l+1} is in hdz[kz]; -1: the rank-1 dy wo of the output layer
     for (int l = HL - 1; l >= 0; --l) {
       const Layer &ly = head[l];
-      run.wgrad(m_z_64[l], m_hdc_64[k], n, M, M, 64, 64, ly.off, partial.p, partial.n, grads.p + ly.w_off,
+      run.wgrad(m_z_64[l], m_hdc_64[kc], n, M, M, 64, 64, ly.off, partial.p, partial.n, grads.p + ly.w_off,
                 grads.p + ly.b_off);
       ConvEpi e{};
-      e.resid_f32 = hdz[k].p;
-      e.out_f32 = hdz[k ^ 1].p;
+      if (kz >= 0) {
+        e.resid_f32 = hdz[kz].p;
+      } else {
+        e.resid_dy = dyb.p;
+        e.wo = params.p + wo_off;
+      }
+      const int oz = kz == 0 ? 1 : 0;
+      e.out_f32 = hdz[oz].p;
       if (l > 0) {
         e.mask_in = hmask[l].p;
-        e.out = hdc[k ^ 1].p;
+        e.out = hdc[kc ^ 1].p;
       }
-      run.conv(m_hdc_128[k], ly.map_wt, n, M, M, 64, 64, negated(ly.off), e);
-      k ^= 1;
+      run.conv(m_hdc_128[kc], ly.map_wt, n, M, M, 64, 64, negated(ly.off), e);
+      kz = oz;
+      kc ^= 1;
     }
+    const int k = kz;  // dz0
     k_pair_bwd<<<dim3(M, n), 256, 0, st>>>(hdz[k].p, uv.p, M, duv.p);
-    k_dist_bwd<<<M, 256, 0, st>>>(hdz[k].p, M, n, grads.p + E_off);
+    k_dist_bwd<<<dim3(M, n), 256, 0, st>>>(hdz[k].p, M, dist_part.p);
+    k_dist_reduce<<<blocks((long long)M * 64), 256, 0, st>>>(dist_part.p, M, n, grads.p + E_off);
     SCK(cudaGetLastError());
-    run.kernels += 2;
+    run.kernels += 3;
     run.wgrad(m_hp_64, m_duv_64, n, 1, M, 128, 128, proj.off, partial.p, partial.n, grads.p + proj.w_off,
               grads.p + proj.b_off);
     {
@@ -607,20 +668,20 @@ struct Net {
     k_unpool<<<blocks((long long)n * L * 8), 256, 0, st>>>(dhp.p, emask[EL].p, L, f, n, edz[0].p, edc[0].p);
     SCK(cudaGetLastError());
     ++run.kernels;
-    k = 0;
+    int ke = 0;
     for (int l = EL - 1; l >= 1; --l) {
       const Layer &ly = enc[l];
-      run.wgrad(m_h_64[l], m_edc_64[k], n, 1, L, 128, 128, ly.off, partial.p, partial.n, grads.p + ly.w_off,
+      run.wgrad(m_h_64[l], m_edc_64[ke], n, 1, L, 128, 128, ly.off, partial.p, partial.n, grads.p + ly.w_off,
                 grads.p + ly.b_off);
       ConvEpi e{};
-      e.resid_f32 = edz[k].p;
-      e.out_f32 = edz[k ^ 1].p;
+      e.resid_f32 = edz[ke].p;
+      e.out_f32 = edz[ke ^ 1].p;
       e.mask_in = emask[l].p;
-      e.out = edc[k ^ 1].p;
-      run.conv(m_edc_128[k], ly.map_wt, n, 1, L, 128, 128, negated(ly.off), e);
-      k ^= 1;
+      e.out = edc[ke ^ 1].p;
+      run.conv(m_edc_128[ke], ly.map_wt, n, 1, L, 128, 128, negated(ly.off), e);
+      ke ^= 1;
     }
-    run.wgrad(m_x0_64, m_edc_64[k], n, 1, L, 64, 128, enc[0].off, partial.p, partial.n, grads.p + enc[0].w_off,
+    run.wgrad(m_x0_64, m_edc_64[ke], n, 1, L, 64, 128, enc[0].off, partial.p, partial.n, grads.p + enc[0].w_off,
               grads.p + enc[0].b_off);
   }
 
@@ -628,14 +689,11 @@ struct Net {
     ++step;
     const float bc1 = 1.0f - std::pow(cfg.beta1, (float)step);
     const float bc2 = 1.0f - std::pow(cfg.beta2, (float)step);
-    for (const Seg &s : segs) {
-      k_adamw<<<blocks((long long)s.n), 256, 0, st>>>(params.p + s.off, grads.p + s.off, adam_m.p + s.off,
-                                                      adam_v.p + s.off, (long long)s.n, cfg.lr, cfg.beta1,
-                                                      cfg.beta2, cfg.adam_eps, s.decay ? cfg.weight_decay : 0.0f,
-                                                      bc1, bc2);
-      SCK(cudaGetLastError());
-      ++run.kernels;
-    }
+    k_adamw<<<blocks((long long)n_params), 256, 0, st>>>(params.p, grads.p, adam_m.p, adam_v.p, decay.p,
+                                                         (long long)n_params, cfg.lr, cfg.beta1, cfg.beta2,
+                                                         cfg.adam_eps, cfg.weight_decay, bc1, bc2);
+    SCK(cudaGetLastError());
+    ++run.kernels;
     refresh_weights();
   }
 
@@ -663,7 +721,7 @@ struct Net {
 
   double loss_grad(const int32_t *rows_host, int n, bool update, bool want_loss) {
     const int32_t *rows = upload_rows(rows_host, n);
-    forward(ds_types.p, ds_lad.p, rows, n);
+    forward(ds_types.p, ds_lad.p, rows, n, true);
     backward(rows, n);
     if (update) adamw();
     double l = 0;
@@ -842,7 +900,7 @@ int ccpsur_predict(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int3
       SCK(cudaMemcpyAsync(n.in_types.p, types + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
       if (lad)
         SCK(cudaMemcpyAsync(n.in_lad.p, lad + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
-      n.forward(n.in_types.p, lad ? n.in_lad.p : nullptr, nullptr, b);
+      n.forward(n.in_types.p, lad ? n.in_lad.p : nullptr, nullptr, b, false);
       n.predict_out(b, maps, first);
     }
     n.check_flags();
@@ -856,7 +914,7 @@ int ccpsur_predict_rows(ccpsur_net *h, const int32_t *rows, int32_t cnt, float *
     for (int32_t first = 0; first < cnt; first += n.cfg.batch) {
       const int b = std::min(n.cfg.batch, cnt - first);
       const int32_t *r = n.upload_rows(rows + first, b);
-      n.forward(n.ds_types.p, n.ds_lad.p, r, b);
+      n.forward(n.ds_types.p, n.ds_lad.p, r, b, false);
       n.predict_out(b, maps, first);
     }
     if (maps) n.check_flags();
@@ -949,7 +1007,7 @@ int ccpsur_conv_bf16(int32_t B, int32_t H, int32_t W, int32_t cin, int32_t cout,
     Launcher run;
     run.st = st;
     run.err = derr.p;
-    CUtensorMap mx = image_map(dx.p, cin, W, H, B, 128);
+    CUtensorMap mx = image_map(dx.p, cin, W, H, B, WIN_ROWS);
     CUtensorMap mw = weight_map(dwb.p, cin, ntaps * cout, cout);
     run.conv(mx, mw, B, H, W, cin, cout, taps, e);
     int flags = 0;

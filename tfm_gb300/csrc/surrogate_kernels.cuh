@@ -4,10 +4,11 @@
 //  * k_conv_tc: implicit-GEMM convolution over channels-last BF16 images
 //    [B][H][W][C]. One CTA tile is 128 consecutive output pixels of one image
 //    row (M = 128) times all output channels (N = 64 or 128); K runs over
-//    taps x 64-channel input blocks. The A operand of each K block is one TMA
-//    load of the input tile shifted by the tap offset (out-of-image pixels
-//    arrive as zeros, which is the convolution's zero padding); the weights of
-//    all taps stay resident in shared memory. Accumulators live in TMEM,
+//    taps x 64-channel input blocks. For each tap row one TMA load brings the
+//    input window of the tile's pixels plus a margin on both sides
+//    (out-of-image pixels arrive as zeros, which is the convolution's zero
+//    padding); each tap of the row reads it at its own row offset. The
+//    weights of all taps stay resident in shared memory. Accumulators live in TMEM,
 //    double-buffered so the epilogue of one tile overlaps the MMAs of the next.
 //    The epilogue fuses bias, ReLU, the residual add, the ReLU mask bits and
 //    the gradient masking of the backward pass. The same kernel computes the
@@ -21,7 +22,8 @@
 //    pixels into FP32 partial sums that k_wgrad_reduce adds up in a fixed
 //    order.
 // CUDA-core kernels: sequence embedding, pooling, the outer-product pair
-// features and their gradient, the output layer with the loss, AdamW.
+// features and their gradient, the loss and its gradient, AdamW. The output
+// layer (64 -> 1) runs in the last head convolution's epilogue.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -34,24 +36,39 @@ namespace sur {
 using bf16 = __nv_bfloat16;
 
 constexpr int MAX_TAPS = 9;
-constexpr int CONV_THREADS = 192;  // warp 0: TMA, warp 1: MMA + TMEM, warps 2-5: epilogue
-constexpr int MAX_STAGES = 4;
-constexpr uint32_t A_TILE = 128u * 128u;  // 128 pixels x 64 BF16 channels
+// warp 0: TMA, warp 1: MMA + TMEM, warps 2-9: epilogue (two warps per TMEM
+// lane quarter, each taking half of the output channels)
+constexpr int CONV_THREADS = 320;
+constexpr int EPI_WARPS = 8;
+constexpr int MAX_STAGES = 8;
 constexpr uint32_t TMEM_COLS_CONV = 256;  // two accumulators of up to 128 columns
 
+// A-operand windows: the input pixels [w0 - WIN_RADIUS, w0 + 128 + WIN_RADIUS)
+// of one image row, so that every tap of that row (column offset |dw| <=
+// WIN_RADIUS) is a row-shifted view of the same shared-memory tile. A K-major
+// 128-byte-swizzled operand may start at any row of such a tile: the swizzle
+// is a function of the absolute shared-memory address.
+constexpr int WIN_RADIUS = 8;
+constexpr int WIN_ROWS = 128 + 2 * WIN_RADIUS;
+constexpr uint32_t WIN_BYTES = (uint32_t)WIN_ROWS * 128u;  // a multiple of 1024
+
+// Taps form an R x C grid (R in {1, 3}, C in {1, 5, ...}, both odd): tap
+// t = r C + c reads the input at (dh, dw) = ((r - R/2) step_h, (c - C/2)
+// step_w). The steps carry the dilation and its sign (negative for the
+// input-gradient convolution); |dw| <= WIN_RADIUS.
 struct ConvShape {
   int B, H, W;     // image (input = output size); W is a multiple of 128
-  int cin_blocks;  // input channels / 64
-  int N;           // output channels: 64 or 128
-  int ntaps;
-  int stages;      // A-operand pipeline depth (2..4)
+  int stages;      // A-window pipeline depth (2..MAX_STAGES)
   int n_tiles;     // B * H * W / 128
-  int dh[MAX_TAPS], dw[MAX_TAPS];  // input offset of each tap (row, column)
+  int step_h, step_w;
 };
 
 // Fused epilogue of k_conv_tc; every pointer is optional. Per output value:
 // v = acc + bias; mask bit = v > 0; v = relu(v); v += resid (BF16 or FP32);
-// out_f32 = v; out = v, zeroed where the bit of mask_in is clear.
+// v += resid_dy[p] wo[c]; out_f32 = v; out = v, zeroed where the bit of
+// mask_in is clear;
+// y[p] += wo . bf16(v[p]) + bo[0] (the network's output layer, N = 64 only;
+// y must be zeroed before the launch).
 struct ConvEpi {
   const float *bias;        // [N]
   int relu;
@@ -61,10 +78,18 @@ struct ConvEpi {
   const uint32_t *mask_in;  // [P][N / 32]
   bf16 *out;                // [P][N]
   uint32_t *mask_out;       // [P][N / 32]
+  const float *wo, *bo;     // [64], [1]
+  float *y;                 // [P]
+  const float *resid_dy;    // [P]: adds resid_dy[p] * wo[c] (the output layer's gradient)
 };
 
+// shared memory after the operand tiles: barriers (256 B), TMEM slot and
+// abort flag (256 B), bias [128], output weights [64]
+constexpr uint32_t CONV_SMEM_TAIL = 256u + 256u + 512u + 256u;
+
 __host__ __device__ constexpr uint32_t conv_smem_bytes(int ntaps, int cin_blocks, int N, int stages) {
-  return 1024u + (uint32_t)(ntaps * cin_blocks) * (uint32_t)N * 128u + (uint32_t)stages * A_TILE + 256u;
+  return 1024u + (uint32_t)(ntaps * cin_blocks) * (uint32_t)N * 128u + (uint32_t)stages * WIN_BYTES +
+         CONV_SMEM_TAIL;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -101,78 +126,125 @@ __device__ __forceinline__ void store_bf16x16(bf16 *dst, const float *v) {
   d[1] = b;
 }
 
-__device__ __forceinline__ void conv_epilogue16(const ConvEpi &e, size_t p, int N, int c0, float *v,
-                                                uint32_t &mask_lo) {
-  const size_t o = p * (size_t)N + c0;
-  if (e.bias) {
+// Epilogue of one output pixel p for the thread's half of the N channels
+// (32 N / 64 columns from TMEM address taddr): all global loads of the row
+// are issued before the accumulator is read so their latencies overlap.
+// Returns this thread's partial output-layer dot (0 without wo).
+template <int N>
+__device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float *sbias, const float *swo,
+                                                   size_t p, int half, uint32_t taddr) {
+  constexpr int G = N / 64;  // 32-column groups per thread
+  const int c_begin = half * (N / 2);
+  uint4 rb[G][4];
+  float4 rf[G][8];
+  uint32_t mi[G];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] += __ldg(e.bias + c0 + i);
+  for (int g = 0; g < G; ++g) {
+    const size_t o = p * (size_t)N + c_begin + 32 * g;
+    if (e.resid) {
+      const uint4 *s = reinterpret_cast<const uint4 *>(e.resid + o);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) rb[g][i] = s[i];
+    }
+    if (e.resid_f32) {
+      const float4 *s = reinterpret_cast<const float4 *>(e.resid_f32 + o);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) rf[g][i] = s[i];
+    }
+    if (e.mask_in) mi[g] = e.mask_in[p * (N / 32) + (c_begin >> 5) + g];
   }
-  if (e.mask_out) {
-    uint32_t bits = 0;
+  const float rdy = e.resid_dy ? e.resid_dy[p] : 0.0f;
+  float dot = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) bits |= (v[i] > 0.0f ? 1u : 0u) << i;
-    if ((c0 & 16) == 0)
-      mask_lo = bits;
-    else
-      e.mask_out[p * (size_t)(N >> 5) + (c0 >> 5)] = mask_lo | (bits << 16);
-  }
-  if (e.relu) {
+  for (int g = 0; g < G; ++g) {
+    const int c0 = c_begin + 32 * g;
+    float v[32];
+    tc::tmem_ld32(taddr + (uint32_t)c0, v);
+    if (e.bias) {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.0f);
-  }
-  if (e.resid) {
-    float r[16];
-    load_bf16x16(e.resid + o, r);
+      for (int i = 0; i < 32; ++i) v[i] += sbias[c0 + i];
+    }
+    if (e.mask_out) {
+      uint32_t bits = 0;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] += r[i];
-  }
-  if (e.resid_f32) {
-    const float4 *r = reinterpret_cast<const float4 *>(e.resid_f32 + o);
+      for (int i = 0; i < 32; ++i) bits |= (v[i] > 0.0f ? 1u : 0u) << i;
+      e.mask_out[p * (N / 32) + (c0 >> 5)] = bits;
+    }
+    if (e.relu) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      float4 x = r[i];
-      v[4 * i] += x.x;
-      v[4 * i + 1] += x.y;
-      v[4 * i + 2] += x.z;
-      v[4 * i + 3] += x.w;
+      for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.0f);
+    }
+    if (e.resid) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t w[4] = {rb[g][i].x, rb[g][i].y, rb[g][i].z, rb[g][i].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          v[8 * i + 2 * k] += bf_lo(w[k]);
+          v[8 * i + 2 * k + 1] += bf_hi(w[k]);
+        }
+      }
+    }
+    if (e.resid_f32) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        v[4 * i] += rf[g][i].x;
+        v[4 * i + 1] += rf[g][i].y;
+        v[4 * i + 2] += rf[g][i].z;
+        v[4 * i + 3] += rf[g][i].w;
+      }
+    }
+    if (e.resid_dy) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = fmaf(rdy, swo[c0 + i], v[i]);
+    }
+    const size_t o = p * (size_t)N + c0;
+    if (e.out_f32) {
+      float4 *d = reinterpret_cast<float4 *>(e.out_f32 + o);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) d[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+    if (e.y) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dot = fmaf(swo[c0 + i], __bfloat162float(__float2bfloat16_rn(v[i])), dot);
+    }
+    if (e.mask_in) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = ((mi[g] >> i) & 1u) ? v[i] : 0.0f;
+    }
+    if (e.out) {
+      store_bf16x16(e.out + o, v);
+      store_bf16x16(e.out + o + 16, v + 16);
     }
   }
-  if (e.out_f32) {
-    float4 *d = reinterpret_cast<float4 *>(e.out_f32 + o);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) d[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-  }
-  if (e.mask_in) {
-    const uint32_t w = e.mask_in[p * (size_t)(N >> 5) + (c0 >> 5)] >> (c0 & 16);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = ((w >> i) & 1u) ? v[i] : 0.0f;
-  }
-  if (e.out) store_bf16x16(e.out + o, v);
+  return dot;
 }
 
 // Implicit-GEMM convolution (see the file comment). tmx: 4-D map over the
 // input image {C, W, H, B} with box {64, 128, 1, 1}; tmw: 2-D map over the
 // weights {C_in, taps x N} with box {64, N}, both with 128-byte swizzle.
 // Grid: persistent, at most one CTA per SM; tiles strided by gridDim.x.
+template <int N, int R, int C, int CB>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
               const ConvShape sh, const ConvEpi epi, int *err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = tc::smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
-  const int nkb = sh.ntaps * sh.cin_blocks;
+  constexpr int nwt = R * C * CB;  // resident weight tiles
   const int S = sh.stages;
-  const int N = sh.N;
   const uint32_t w_tile = (uint32_t)N * 128u;
   const uint32_t w_base = base;
-  const uint32_t a_base = w_base + (uint32_t)nkb * w_tile;
-  const uint32_t bar0 = a_base + (uint32_t)S * A_TILE;
+  const uint32_t a_base = w_base + (uint32_t)nwt * w_tile;
+  const uint32_t bar0 = a_base + (uint32_t)S * WIN_BYTES;
   // barriers: full[S], empty[S], tfull[2], tempty[2], weights, fin
   const uint32_t full0 = bar0, empty0 = bar0 + 8u * S, tfull0 = bar0 + 16u * S,
                  tempty0 = tfull0 + 16u, wbar = tempty0 + 16u, fin = wbar + 8u;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem_raw + (fin + 8u - raw));
+  uint8_t *tail = smem_raw + (bar0 + 256u - raw);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tail);
   volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  float *sbias = reinterpret_cast<float *>(tail + 256);
+  float *swo = sbias + 128;  // [64]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -182,13 +254,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(tfull0 + 8u * b, 1);
-      tc::mbar_init(tempty0 + 8u * b, 4);
+      tc::mbar_init(tempty0 + 8u * b, EPI_WARPS);
     }
     tc::mbar_init(wbar, 1);
     tc::mbar_init(fin, 1);
     *abort = 0;
     tc::fence_barrier_init();
   }
+  for (int k = threadIdx.x; k < N; k += blockDim.x) sbias[k] = epi.bias ? epi.bias[k] : 0.0f;
+  for (int k = threadIdx.x; k < 64; k += blockDim.x) swo[k] = epi.wo ? epi.wo[k] : 0.0f;
   if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), TMEM_COLS_CONV);
   tc::fence_before_sync();
   __syncthreads();
@@ -201,62 +275,85 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       // ---- TMA producer: resident weights once, then one A tile per K block
       tc::prefetch_map(&tmx);
       tc::prefetch_map(&tmw);
-      tc::mbar_arrive_expect_tx(wbar, (uint32_t)nkb * w_tile);
-      for (int t = 0; t < sh.ntaps; ++t)
-        for (int cb = 0; cb < sh.cin_blocks; ++cb)
-          tc::tma_load_2d(w_base + (uint32_t)(t * sh.cin_blocks + cb) * w_tile, &tmw, wbar, cb * 64,
-                          t * N);
-      uint32_t it = 0;
+      tc::mbar_arrive_expect_tx(wbar, (uint32_t)nwt * w_tile);
+      for (int t = 0; t < R * C; ++t)
+        for (int cb = 0; cb < CB; ++cb)
+          tc::tma_load_2d(w_base + (uint32_t)(t * CB + cb) * w_tile, &tmw, wbar, cb * 64, t * N);
+      int s = 0;
+      uint32_t ph = 0;
+      uint32_t issued = 0;
       for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x) {
         const int wb = tile % wtiles, bh = tile / wtiles;
         const int h = bh % sh.H, b = bh / sh.H;
-        for (int t = 0; t < sh.ntaps; ++t)
-          for (int cb = 0; cb < sh.cin_blocks; ++cb) {
-            const int s = (int)(it % (uint32_t)S);
-            const uint32_t r = it / (uint32_t)S;
-            if (!tc::mbar_wait(empty0 + 8u * s, (r & 1u) ^ 1u, abort)) goto produced;
-            tc::mbar_arrive_expect_tx(full0 + 8u * s, A_TILE);
-            tc::tma_load_4d(a_base + (uint32_t)s * A_TILE, &tmx, full0 + 8u * s, cb * 64,
-                            wb * 128 + sh.dw[t], h + sh.dh[t], b);
-            ++it;
+        for (int r = 0; r < R; ++r)
+          for (int cb = 0; cb < CB; ++cb) {
+            if (!tc::mbar_wait(empty0 + 8u * s, ph ^ 1u, abort)) goto produced;
+            tc::mbar_arrive_expect_tx(full0 + 8u * s, WIN_BYTES);
+            tc::tma_load_4d(a_base + (uint32_t)s * WIN_BYTES, &tmx, full0 + 8u * s, cb * 64,
+                            wb * 128 - WIN_RADIUS, h + (r - R / 2) * sh.step_h, b);
+            ++issued;
+            if (++s == S) {
+              s = 0;
+              ph ^= 1u;
+            }
           }
       }
     produced:
-      // nothing may still be landing in shared memory when the CTA exits
+      // nothing may still be landing in shared memory when the CTA exits:
+      // wait for the last (up to S) windows issued, newest first
       tc::mbar_drain(wbar, 0);
-      for (uint32_t k = (it > (uint32_t)S ? it - (uint32_t)S : 0u); k < it; ++k)
-        tc::mbar_drain(full0 + 8u * (k % (uint32_t)S), (k / (uint32_t)S) & 1u);
+      for (uint32_t k = 0; k < issued && k < (uint32_t)S; ++k) {
+        if (--s < 0) {
+          s = S - 1;
+          ph ^= 1u;
+        }
+        tc::mbar_drain(full0 + 8u * s, ph);
+      }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer
-      const uint32_t idesc = tc::idesc_bf16(128, N, false, false);
-      uint32_t it = 0;
+      constexpr uint32_t idesc = tc::idesc_bf16(128, N, false, false);
+      // descriptor bits other than the start address (bits 0-13; shared
+      // memory addresses are below 2^18)
+      const uint64_t desc_hi = tc::sdesc(0u, 16u, 1024u);
+      int s = 0;
+      uint32_t ph = 0;
       int local = 0;
       if (tc::mbar_wait(wbar, 0, abort)) {
         for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
           const int buf = local & 1;
-          const uint32_t use = (uint32_t)local >> 1;
-          if (!tc::mbar_wait(tempty0 + 8u * buf, (use & 1u) ^ 1u, abort)) break;
+          if (!tc::mbar_wait(tempty0 + 8u * buf, (((uint32_t)local >> 1) & 1u) ^ 1u, abort)) break;
           tc::fence_after_sync();
           const uint32_t d = tmem + (uint32_t)(buf * N);
+          uint32_t acc = 0;
           bool ok = true;
-          for (int kb = 0; kb < nkb; ++kb, ++it) {
-            const int s = (int)(it % (uint32_t)S);
-            const uint32_t r = it / (uint32_t)S;
-            if (!tc::mbar_wait(full0 + 8u * s, r & 1u, abort)) {
-              ok = false;
-              break;
-            }
-            tc::fence_after_sync();
-            const uint32_t a0 = a_base + (uint32_t)s * A_TILE;
-            const uint32_t b0 = w_base + (uint32_t)kb * w_tile;
+#pragma unroll 1
+          for (int r = 0; r < R && ok; ++r)
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-              tc::mma_bf16(d, tc::sdesc(a0 + 32u * k, 16u, 1024u), tc::sdesc(b0 + 32u * k, 16u, 1024u),
-                           idesc, (kb | k) != 0 ? 1u : 0u);
-            tc::mma_commit(empty0 + 8u * s);
-          }
+            for (int cb = 0; cb < CB; ++cb) {
+              if (!tc::mbar_wait(full0 + 8u * s, ph, abort)) {
+                ok = false;
+                break;
+              }
+              tc::fence_after_sync();
+              const uint32_t win = a_base + (uint32_t)s * WIN_BYTES;
+#pragma unroll
+              for (int c = 0; c < C; ++c) {
+                const uint32_t a0 = win + (uint32_t)(WIN_RADIUS + (c - C / 2) * sh.step_w) * 128u;
+                const uint32_t b0 = w_base + (uint32_t)(((r * C + c) * CB + cb)) * w_tile;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                  tc::mma_bf16(d, desc_hi | ((a0 + 32u * k) >> 4), desc_hi | ((b0 + 32u * k) >> 4), idesc, acc);
+                  acc = 1;
+                }
+              }
+              tc::mma_commit(empty0 + 8u * s);
+              if (++s == S) {
+                s = 0;
+                ph ^= 1u;
+              }
+            }
           if (!ok) break;
           tc::mma_commit(tfull0 + 8u * buf);
         }
@@ -265,8 +362,9 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       tc::mbar_drain(fin, 0);
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31
+    // ---- epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31, half of the columns
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     int local = 0;
     for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
@@ -277,15 +375,13 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       const int wb = tile % wtiles, bh = tile / wtiles;
       const size_t p = (size_t)bh * sh.W + (size_t)wb * 128 + row;
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N);
-      uint32_t mask_lo = 0;
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(taddr + (uint32_t)c0, v);
-        conv_epilogue16(epi, p, N, c0, v, mask_lo);
-      }
+      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tempty0 + 8u * buf);
+      // the two halves of a row add their partial dots to the zeroed y: a sum
+      // of two terms onto zero does not depend on their order
+      if (epi.y) atomicAdd(epi.y + p, half == 0 ? dot + epi.bo[0] : dot);
     }
   }
   tc::fence_before_sync();
@@ -454,25 +550,29 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
   if (threadIdx.x == 0 && *abort) atomicOr(err, 2);
 }
 
-// dW[tap][co][ci] = sum over chunks of the X atoms' partials, in chunk order;
-// db[co] from the first all-ones atom. cin_blocks: input channel blocks
-// (X atom a = tap * cin_blocks + block).
-__global__ void k_wgrad_reduce(const float *__restrict__ partial, int chunks, int n_atoms, int n_x,
-                               int N, int cin_blocks, float *__restrict__ dw, float *__restrict__ db) {
-  const int cin = cin_blocks * 64;
-  const int total = n_x * N * 64;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < total) {
-    const int ci = k & 63, co = (k >> 6) % N, a = k / (64 * N);
-    float s = 0.0f;
-    for (int c = 0; c < chunks; ++c) s += partial[((size_t)c * n_atoms + a) * (size_t)N * 64 + (size_t)co * 64 + ci];
+// dW[tap][co][ci] = sum over chunks of the X atoms' partials, in chunk order
+// per thread group and then over the 4 groups; db[co] from the first all-ones
+// atom. cin_blocks: input channel blocks (X atom a = tap * cin_blocks +
+// block). Block (64 x 4 threads): one (atom, co) row of 64 entries;
+// blockIdx.x = atom * N + co, and n_x * N + co for the bias.
+__global__ void __launch_bounds__(256)
+    k_wgrad_reduce(const float *__restrict__ partial, int chunks, int n_atoms, int n_x, int N, int cin_blocks,
+                   float *__restrict__ dw, float *__restrict__ db) {
+  const int ci = threadIdx.x & 63, g = threadIdx.x >> 6;
+  const int a = blockIdx.x / N, co = blockIdx.x - a * N;  // a == n_x: the bias row
+  float s = 0.0f;
+  for (int c = g; c < chunks; c += 4) s += partial[((size_t)c * n_atoms + a) * (size_t)N * 64 + (size_t)co * 64 + ci];
+  __shared__ float r[4][64];
+  r[g][ci] = s;
+  __syncthreads();
+  if (g) return;
+  const float v = (r[0][ci] + r[1][ci]) + (r[2][ci] + r[3][ci]);
+  if (a < n_x) {
+    const int cin = cin_blocks * 64;
     const int tap = a / cin_blocks, blk = a - tap * cin_blocks;
-    dw[((size_t)tap * N + co) * cin + blk * 64 + ci] = s;
-  } else if (db && k < total + N) {
-    const int co = k - total;
-    float s = 0.0f;
-    for (int c = 0; c < chunks; ++c) s += partial[((size_t)c * n_atoms + n_x) * (size_t)N * 64 + (size_t)co * 64];
-    db[co] = s;
+    dw[((size_t)tap * N + co) * cin + blk * 64 + ci] = v;
+  } else if (ci == 0) {
+    db[co] = v;
   }
 }
 
@@ -512,44 +612,45 @@ __global__ void k_pool(const bf16 *__restrict__ h, int L, int C, int f, int n, b
 }
 
 // Pair features of the head input: z0[b][i][j][c] = u_i[c] v_j[c] + u_j[c] v_i[c]
-// + E[|i - j|][c], u = uv[..][0, 64), v = uv[..][64, 128). Block: one row i.
+// + E[|i - j|][c], u = uv[..][0, 64), v = uv[..][64, 128). Block: PAIR_ROWS
+// consecutive rows i of one sample, so each u_j, v_j read serves them all.
+constexpr int PAIR_ROWS = 8;
+
 __global__ void __launch_bounds__(256)
     k_pair_fwd(const bf16 *__restrict__ uv, const float *__restrict__ E, int M, bf16 *__restrict__ z0) {
-  const int i = blockIdx.x, b = blockIdx.y;
-  __shared__ float ui[64], vi[64];
-  const bf16 *row = uv + ((size_t)b * M + i) * 128;
-  if (threadIdx.x < 64) {
-    ui[threadIdx.x] = __bfloat162float(row[threadIdx.x]);
-    vi[threadIdx.x] = __bfloat162float(row[64 + threadIdx.x]);
+  const int i0 = blockIdx.x * PAIR_ROWS, b = blockIdx.y;
+  __shared__ __align__(16) float ui[PAIR_ROWS][64], vi[PAIR_ROWS][64];
+  for (int k = threadIdx.x; k < PAIR_ROWS * 64; k += blockDim.x) {
+    const int r = k >> 6, c = k & 63;
+    const bf16 *row = uv + ((size_t)b * M + i0 + r) * 128;
+    ui[r][c] = __bfloat162float(row[c]);
+    vi[r][c] = __bfloat162float(row[64 + c]);
   }
   __syncthreads();
-  // thread -> (j, 16-channel chunk)
+  // thread -> (j, 16-channel chunk) for all PAIR_ROWS rows
   for (int k = threadIdx.x; k < M * 4; k += blockDim.x) {
     const int j = k >> 2, c0 = (k & 3) * 16;
     const bf16 *rj = uv + ((size_t)b * M + j) * 128;
     float uj[16], vj[16], v[16];
     load_bf16x16(rj + c0, uj);
     load_bf16x16(rj + 64 + c0, vj);
-    const float *e = E + (size_t)abs(i - j) * 64 + c0;
+#pragma unroll 2
+    for (int r = 0; r < PAIR_ROWS; ++r) {
+      const int i = i0 + r;
+      const float4 *e4 = reinterpret_cast<const float4 *>(E + (size_t)abs(i - j) * 64 + c0);
+      const float4 *u4 = reinterpret_cast<const float4 *>(&ui[r][c0]);
+      const float4 *w4 = reinterpret_cast<const float4 *>(&vi[r][c0]);
 #pragma unroll
-    for (int t = 0; t < 16; ++t) v[t] = fmaf(ui[c0 + t], vj[t], fmaf(uj[t], vi[c0 + t], e[t]));
-    store_bf16x16(z0 + (((size_t)b * M + i) * M + j) * 64 + c0, v);
+      for (int q = 0; q < 4; ++q) {
+        const float4 e = __ldg(e4 + q), a = u4[q], c = w4[q];
+        v[4 * q] = fmaf(a.x, vj[4 * q], fmaf(uj[4 * q], c.x, e.x));
+        v[4 * q + 1] = fmaf(a.y, vj[4 * q + 1], fmaf(uj[4 * q + 1], c.y, e.y));
+        v[4 * q + 2] = fmaf(a.z, vj[4 * q + 2], fmaf(uj[4 * q + 2], c.z, e.z));
+        v[4 * q + 3] = fmaf(a.w, vj[4 * q + 3], fmaf(uj[4 * q + 3], c.w, e.w));
+      }
+      store_bf16x16(z0 + (((size_t)b * M + i) * M + j) * 64 + c0, v);
+    }
   }
-}
-
-// Output layer: y[p] = wo . z[p] + bo over 64 channels; one thread per pixel.
-__global__ void k_head_out(const bf16 *__restrict__ z, const float *__restrict__ wo, const float *__restrict__ bo,
-                           long long P, float *__restrict__ y) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  float s = bo[0];
-  for (int c0 = 0; c0 < 64; c0 += 16) {
-    float v[16];
-    load_bf16x16(z + p * 64 + c0, v);
-#pragma unroll
-    for (int t = 0; t < 16; ++t) s = fmaf(__ldg(wo + c0 + t), v[t], s);
-  }
-  y[p] = s;
 }
 
 // Prediction: symmetrised log map -> contact probability max(exp(yhat) - eps, 0).
@@ -564,12 +665,14 @@ __global__ void k_predict_maps(const float *__restrict__ y, int M, int n, float 
 
 // Loss and the gradient entering the head. yhat = (y + y^T) / 2, loss =
 // mean (yhat - t)^2 over n M^2 values (targets symmetric, so dL/dy = dL/dyhat).
-// Writes dz[p][c] = dy wo[c] (FP32), dc[p][c] = dz masked by the last head
-// layer's ReLU bits (BF16), and accumulates d wo, d bo and the loss.
+// The gradient of the last head output is the rank-1 dz[p][c] = dy[p] wo[c]:
+// only dy is stored (the next convolution's epilogue expands it); dc[p][c] =
+// dz masked by the last head layer's ReLU bits (BF16). Accumulates d wo,
+// d bo and the loss.
 __global__ void __launch_bounds__(256)
     k_loss_out_bwd(const float *__restrict__ y, const float *__restrict__ target, const int32_t *__restrict__ idx,
                    const bf16 *__restrict__ z, const uint32_t *__restrict__ mask, const float *__restrict__ wo,
-                   int M, int n, float *__restrict__ dz, bf16 *__restrict__ dc, float *__restrict__ gwo,
+                   int M, int n, float *__restrict__ dy, bf16 *__restrict__ dc, float *__restrict__ gwo,
                    float *__restrict__ gbo, double *__restrict__ loss) {
   __shared__ float swo[64];
   __shared__ float red[8][65];
@@ -590,6 +693,7 @@ __global__ void __launch_bounds__(256)
     const float d = yh - target[row * MM + r];
     l2 = d * d;
     dyv = 2.0f * d / (float)P;
+    dy[p] = dyv;
     const uint32_t m0 = mask[p * 2], m1 = mask[p * 2 + 1];
     for (int c0 = 0; c0 < 64; c0 += 16) {
       float zv[16], g[16];
@@ -597,14 +701,9 @@ __global__ void __launch_bounds__(256)
       const uint32_t w = (c0 < 32 ? m0 : m1) >> (c0 & 16);
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
-        g[t] = dyv * swo[c0 + t];
+        g[t] = ((w >> t) & 1u) ? dyv * swo[c0 + t] : 0.0f;
         gw[c0 + t] = dyv * zv[t];
       }
-      float4 *o = reinterpret_cast<float4 *>(dz + p * 64 + c0);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) o[t] = make_float4(g[4 * t], g[4 * t + 1], g[4 * t + 2], g[4 * t + 3]);
-#pragma unroll
-      for (int t = 0; t < 16; ++t) g[t] = ((w >> t) & 1u) ? g[t] : 0.0f;
       store_bf16x16(dc + p * 64 + c0, g);
     }
   }
@@ -672,25 +771,32 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Gradient of the distance embedding: dE[s][c] = sum over samples and over
-// pairs with |i - j| = s of dz_ij[c]. Block: one separation s; 64 channels x 4.
+// Gradient of the distance embedding, per sample: part[b][s][c] = sum over
+// pairs with |i - j| = s of dz_ij[c] (both triangles). Block: (s, b); 64
+// channels x 4 groups over i. k_dist_reduce adds the samples in order.
 __global__ void __launch_bounds__(256)
-    k_dist_bwd(const float *__restrict__ dz, int M, int n, float *__restrict__ dE) {
-  const int s = blockIdx.x;
+    k_dist_bwd(const float *__restrict__ dz, int M, float *__restrict__ part) {
+  const int s = blockIdx.x, b = blockIdx.y;
   const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
   const size_t MM = (size_t)M * M;
+  const float *dzb = dz + (size_t)b * MM * 64;
   float acc = 0.0f;
-  for (int b = 0; b < n; ++b) {
-    const float *dzb = dz + (size_t)b * MM * 64;
-    for (int i = g; i + s < M; i += 4) {
-      acc += dzb[((size_t)i * M + i + s) * 64 + c];
-      if (s) acc += dzb[((size_t)(i + s) * M + i) * 64 + c];
-    }
+  for (int i = g; i + s < M; i += 4) {
+    acc += dzb[((size_t)i * M + i + s) * 64 + c];
+    if (s) acc += dzb[((size_t)(i + s) * M + i) * 64 + c];
   }
   __shared__ float r[4][64];
   r[g][c] = acc;
   __syncthreads();
-  if (g == 0) dE[(size_t)s * 64 + c] = r[0][c] + r[1][c] + r[2][c] + r[3][c];
+  if (g == 0) part[((size_t)b * M + s) * 64 + c] = r[0][c] + r[1][c] + r[2][c] + r[3][c];
+}
+
+__global__ void k_dist_reduce(const float *__restrict__ part, int M, int n, float *__restrict__ dE) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= M * 64) return;
+  float s = 0.0f;
+  for (int b = 0; b < n; ++b) s += part[(size_t)b * M * 64 + k];
+  dE[k] = s;
 }
 
 // Unpooling of the projection-input gradient: dz[b][l][c] = dhp[b][l / f][c] / f
@@ -718,10 +824,10 @@ __global__ void k_unpool(const float *__restrict__ dhp, const uint32_t *__restri
   store_bf16x16(dc + bl * 128 + c0, v);
 }
 
-// AdamW on one parameter segment (FP32 master weights).
+// AdamW over the whole FP32 parameter vector; decay[k] selects weight decay.
 __global__ void k_adamw(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
-                        float *__restrict__ v, long long n, float lr, float b1, float b2, float eps,
-                        float wd, float bc1, float bc2) {
+                        float *__restrict__ v, const uint8_t *__restrict__ decay, long long n, float lr, float b1,
+                        float b2, float eps, float wd, float bc1, float bc2) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const float gk = g[k];
@@ -730,19 +836,29 @@ __global__ void k_adamw(float *__restrict__ p, const float *__restrict__ g, floa
   m[k] = mk;
   v[k] = vk;
   const float upd = (mk / bc1) / (sqrtf(vk / bc2) + eps);
-  p[k] = p[k] * (1.0f - lr * wd) - lr * upd;
+  p[k] = p[k] * (1.0f - lr * (decay[k] ? wd : 0.0f)) - lr * upd;
 }
 
-// BF16 copies of a convolution's weights: W [taps][co][ci] and the transposed
-// WT [taps][ci][co] used by the input-gradient convolution.
-__global__ void k_weights_bf16(const float *__restrict__ w, int taps, int co, int ci, bf16 *__restrict__ wb,
-                               bf16 *__restrict__ wt) {
+// BF16 copies of every convolution's weights: W [taps][co][ci] and the
+// transposed WT [taps][ci][co] used by the input-gradient convolution.
+// blockIdx.y selects the layer.
+constexpr int MAX_LAYERS = 80;
+struct WeightTable {
+  int n;
+  int taps[MAX_LAYERS], co[MAX_LAYERS], ci[MAX_LAYERS];
+  long long off[MAX_LAYERS];
+  bf16 *wb[MAX_LAYERS], *wt[MAX_LAYERS];
+};
+
+__global__ void k_weights_bf16(const float *__restrict__ params, const __grid_constant__ WeightTable t) {
+  const int l = blockIdx.y;
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int taps = t.taps[l], co = t.co[l], ci = t.ci[l];
   if (k >= (long long)taps * co * ci) return;
-  const int i = (int)(k % ci), o = (int)((k / ci) % co), t = (int)(k / ((long long)ci * co));
-  const bf16 x = __float2bfloat16_rn(w[k]);
-  wb[k] = x;
-  wt[((long long)t * ci + i) * co + o] = x;
+  const int i = (int)(k % ci), o = (int)((k / ci) % co), tp = (int)(k / ((long long)ci * co));
+  const bf16 x = __float2bfloat16_rn(params[t.off[l] + k]);
+  t.wb[l][k] = x;
+  t.wt[l][((long long)tp * ci + i) * co + o] = x;
 }
 
 }  // namespace sur
