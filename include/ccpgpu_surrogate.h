@@ -19,10 +19,20 @@
  *             u_j v_i + E[|i - j|] (E learned, bins x 64)
  *   head      head_layers [6] residual 3x3 convolutions, width 64, dilations
  *             [1,2,4,8,1,2]
- *   output    y = w . z + b; yhat = (y + y^T) / 2 predicts log(p + target_eps)
- * Loss: mean squared error of yhat against log(p + target_eps). Optimiser:
+ *   output    y = w . z + b; yhat = (y + y^T) / 2 predicts log p, the map is
+ *             exp(min(yhat, 0)); the loss gradient passes the clamp unchanged
+ * Loss: the Poisson deviance of the observed probability p against exp(yhat),
+ * w[s] (exp(yhat) - p - p (yhat - log p)) averaged over all values, weighted
+ * per separation s = |i - j| by w[s] = bins / (P(s) x pairs(s)), P(s) the
+ * dataset's mean contact probability at s (floored at 1e-6) and pairs(s) the
+ * bin pairs at s, so that every separation carries the same weight. Optimiser:
  * AdamW (lr [1e-3], beta1 [0.9], beta2 [0.999], adam_eps [1e-8],
- * weight_decay [0.01] on weight matrices). Weights are FP32 masters with BF16
+ * weight_decay [0.01] on weight matrices) after the gradient is clipped to a
+ * global L2 norm of clip_norm [1] (0: no clip); with lr_steps > 0 the
+ * learning rate decays from lr to lr_min [0] along a half cosine over the
+ * first lr_steps steps and stays at lr_min after. The output weights start at
+ * zero and the output bias at the log of the dataset's mean contact
+ * probability. Weights are FP32 masters with BF16
  * copies; activations BF16; every contraction accumulates in FP32.
  *
  * Status codes and ccpgpu_last_error() are those of ccpgpu.h. A handle owns
@@ -69,7 +79,9 @@ int ccpsur_get_grads(ccpsur_net *h, float *out, int64_t n);
 
 /* Training set, copied to the device: types [n][seq_len] (0 = A, 1 = B), lad
  * [n][seq_len] (nonzero = LAD bead, may be NULL), maps [n][bins][bins]
- * contact probabilities (symmetric). */
+ * contact probabilities in [0, 1] (symmetric). Sets the separation weights of
+ * the loss and, before the first optimiser step, starts the output bias at
+ * the log of the mean contact probability. */
 int ccpsur_set_dataset(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, const float *maps,
                        int32_t n);
 

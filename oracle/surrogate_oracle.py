@@ -21,7 +21,8 @@ import numpy as np
 import torch
 
 DEFAULTS = dict(seq_len=1024, bins=256, batch=32, enc_layers=8, enc_width=128, enc_kernel=5,
-                head_layers=6, head_width=64, dilations=(1, 2, 4, 8, 1, 2), target_eps=1e-3)
+                head_layers=6, head_width=64, dilations=(1, 2, 4, 8, 1, 2))
+YHAT_MAX = 0.0
 
 
 def config(**kw):
@@ -138,13 +139,35 @@ def symmetric(y):
     return 0.5 * (y + y.transpose(1, 2))
 
 
-def loss_and_grads(flat, cfg, types, lad, maps):
-    """Mean squared error of yhat against log(p + target_eps); FP64 loss and
-    flat gradient."""
+def separation_weights(dataset_maps):
+    """w[s] = M / (P(s) x bin pairs at separation s), P(s) the dataset's mean
+    contact probability at |i - j| = s floored at 1e-6 (ccpsur_set_dataset):
+    every separation carries the same total weight."""
+    m = np.asarray(dataset_maps, np.float64)
+    n, M, _ = m.shape
+    i = np.arange(M)
+    dist = np.abs(i[:, None] - i[None, :])
+    tot = np.bincount(dist.ravel(), weights=m.sum(axis=0).ravel(), minlength=M)
+    npairs = np.bincount(dist.ravel(), minlength=M).astype(np.float64)
+    return M / (np.maximum(tot / (n * npairs), 1e-6) * npairs)
+
+
+def loss_and_grads(flat, cfg, types, lad, maps, dataset_maps):
+    """Separation-weighted Poisson deviance of the maps against exp(yhat),
+    mean over all values; FP64 loss and flat gradient. dataset_maps: every
+    map given to ccpsur_set_dataset (they set the weights)."""
     leaf, p = unpack(flat, cfg)
     y = forward(p, cfg, types, lad)
-    t = torch.log(torch.as_tensor(np.asarray(maps, np.float64)) + cfg["target_eps"])
-    loss = ((symmetric(y) - t) ** 2).mean()
+    t = torch.as_tensor(np.asarray(maps, np.float64))
+    M = cfg["bins"]
+    idx = np.arange(M)
+    w = torch.as_tensor(separation_weights(dataset_maps).astype(np.float32).astype(np.float64))
+    wmat = w[torch.as_tensor(np.abs(idx[:, None] - idx[None, :]))]
+    ys = symmetric(y)
+    # clamped forward, straight-through backward (as the GPU loss kernel)
+    yh = ys - (ys - torch.clamp(ys, max=YHAT_MAX)).detach()
+    dev = torch.exp(yh) - t - t * yh + torch.xlogy(t, t)
+    loss = (wmat[None] * dev).mean()
     loss.backward()
     return float(loss.detach()), leaf.grad.numpy().copy()
 
@@ -153,4 +176,4 @@ def predict(flat, cfg, types, lad):
     with torch.no_grad():
         _, p = unpack(flat, cfg)
         yh = symmetric(forward(p, cfg, types, lad))
-        return torch.clamp(torch.exp(yh) - cfg["target_eps"], min=0.0).numpy()
+        return torch.exp(torch.clamp(yh, max=YHAT_MAX)).numpy()

@@ -280,7 +280,9 @@ struct Config {
   int head_layers = 6, head_width = 64;
   std::vector<int> dilations = {1, 2, 4, 8, 1, 2};
   float lr = 1e-3f, beta1 = 0.9f, beta2 = 0.999f, adam_eps = 1e-8f, weight_decay = 0.01f;
-  float target_eps = 1e-3f;
+  float clip_norm = 1.0f;  // global gradient-norm clip before AdamW; 0: none
+  long long lr_steps = 0;  // cosine decay of lr to lr_min over this many steps; 0: constant
+  float lr_min = 0.0f;
 };
 
 static Config parse_config(const std::string &text) {
@@ -299,7 +301,9 @@ static Config parse_config(const std::string &text) {
   c.beta2 = pm.get<float>("beta2", c.beta2);
   c.adam_eps = pm.get<float>("adam_eps", c.adam_eps);
   c.weight_decay = pm.get<float>("weight_decay", c.weight_decay);
-  c.target_eps = pm.get<float>("target_eps", c.target_eps);
+  c.clip_norm = pm.get<float>("clip_norm", c.clip_norm);
+  c.lr_steps = (long long)pm.get<int>("lr_steps", 0);
+  c.lr_min = pm.get<float>("lr_min", c.lr_min);
   if (pm.has("dilations")) {
     c.dilations.clear();
     std::string s = pm.raw("dilations");
@@ -324,7 +328,9 @@ static Config parse_config(const std::string &text) {
   if ((int)c.dilations.size() != c.head_layers) fail("dilations must list one value per head layer");
   for (int d : c.dilations)
     if (d < 1 || d > WIN_RADIUS) fail("dilation out of range");
-  if (!(c.lr > 0) || !(c.target_eps > 0)) fail("lr and target_eps must be positive");
+  if (!(c.lr > 0)) fail("lr must be positive");
+  if (!(c.clip_norm >= 0)) fail("clip_norm must be >= 0");
+  if (c.lr_steps < 0 || !(c.lr_min >= 0) || c.lr_min > c.lr) fail("lr schedule out of range");
   return c;
 }
 
@@ -360,7 +366,7 @@ struct Net {
   Buf<float> hdz[2], edz[2], dhp;
   Buf<bf16> hdc[2], edc[2], duv;
   Buf<float> partial;
-  Buf<double> loss;
+  Buf<double> loss, gsq;
   Buf<int> err;
   // tensor maps: *128 for the convolution (box of WIN_ROWS pixels: a tile of
   // 128 plus the tap margin), *64 for the weight gradient (box of 64 pixels)
@@ -369,7 +375,7 @@ struct Net {
   CUtensorMap m_hdc_64[2]{}, m_hdc_128[2]{}, m_edc_64[2]{}, m_edc_128[2]{};
   // dataset
   Buf<uint8_t> ds_types, ds_lad;
-  Buf<float> ds_target;
+  Buf<float> ds_target, ds_sweight;
   int ds_n = 0;
   Buf<int32_t> d_rows;
   Buf<uint8_t> in_types, in_lad;
@@ -446,6 +452,7 @@ struct Net {
     refresh_weights();
     alloc_activations();
     loss.alloc(1);
+    gsq.alloc(1);
     err.alloc(1);
     err.zero(st);
     run.err = err.p;
@@ -486,8 +493,9 @@ struct Net {
     fill(proj, 1.0f / std::sqrt(128.0f), 128);
     for (int l = 0; l < cfg.head_layers; ++l)
       fill(head[l], std::sqrt(2.0f / (64.0f * 9.0f)) / std::sqrt((float)cfg.head_layers), 64);
-    for (int c = 0; c < 64; ++c) p[wo_off + c] = 0.05f * nd(rng);
-    p[bo_off] = std::log(cfg.target_eps);
+    // output weights start at zero: the first prediction is the output bias
+    // (the log of the dataset's mean contact probability) everywhere
+    p[bo_off] = std::log(1e-3f);
     SCK(cudaMemcpyAsync(params.p, p.data(), n_params * sizeof(float), cudaMemcpyHostToDevice, st));
     SCK(cudaStreamSynchronize(st));
   }
@@ -624,8 +632,9 @@ struct Net {
     SCK(cudaMemsetAsync(loss.p, 0, sizeof(double), st));
     const long long P = (long long)n * M * M;
     const int HL = cfg.head_layers;
-    k_loss_out_bwd<<<blocks(P), 256, 0, st>>>(y.p, ds_target.p, rows, z[HL].p, hmask[HL].p, params.p + wo_off, M, n,
-                                              dyb.p, hdc[0].p, grads.p + wo_off, grads.p + bo_off, loss.p);
+    k_loss_out_bwd<<<blocks(P), 256, 0, st>>>(y.p, ds_target.p, ds_sweight.p, rows, z[HL].p, hmask[HL].p,
+                                              params.p + wo_off, M, n, dyb.p, hdc[0].p, grads.p + wo_off,
+                                              grads.p + bo_off, loss.p);
     SCK(cudaGetLastError());
     ++run.kernels;
     int kc = 0;   // dc_l is in hdc[kc]
@@ -689,11 +698,20 @@ struct Net {
     ++step;
     const float bc1 = 1.0f - std::pow(cfg.beta1, (float)step);
     const float bc2 = 1.0f - std::pow(cfg.beta2, (float)step);
+    float lr = cfg.lr;
+    if (cfg.lr_steps > 0) {
+      const double f = std::min(1.0, (double)(step - 1) / (double)cfg.lr_steps);
+      lr = (float)(cfg.lr_min + 0.5 * (cfg.lr - cfg.lr_min) * (1.0 + std::cos(3.14159265358979323846 * f)));
+    }
+    SCK(cudaMemsetAsync(gsq.p, 0, sizeof(double), st));
+    k_grad_sq<<<std::min<long long>(blocks((long long)n_params), 1024), 256, 0, st>>>(grads.p, (long long)n_params,
+                                                                                       gsq.p);
     k_adamw<<<blocks((long long)n_params), 256, 0, st>>>(params.p, grads.p, adam_m.p, adam_v.p, decay.p,
-                                                         (long long)n_params, cfg.lr, cfg.beta1, cfg.beta2,
-                                                         cfg.adam_eps, cfg.weight_decay, bc1, bc2);
+                                                         (long long)n_params, lr, cfg.beta1, cfg.beta2,
+                                                         cfg.adam_eps, cfg.weight_decay, bc1, bc2, cfg.clip_norm,
+                                                         gsq.p);
     SCK(cudaGetLastError());
-    ++run.kernels;
+    run.kernels += 2;
     refresh_weights();
   }
 
@@ -734,7 +752,7 @@ struct Net {
 
   void predict_out(int n, float *maps_host, size_t first) {
     const long long P = (long long)n * M * M;
-    k_predict_maps<<<blocks(P), 256, 0, st>>>(y.p, M, n, cfg.target_eps, pred.p);
+    k_predict_maps<<<blocks(P), 256, 0, st>>>(y.p, M, n, pred.p);
     SCK(cudaGetLastError());
     ++run.kernels;
     if (maps_host)
@@ -843,14 +861,24 @@ int ccpsur_set_dataset(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, 
   return sguard([&] {
     Net &n = net_of(h);
     sneed(types && maps && cnt > 0, "null argument or empty dataset");
-    const size_t L = n.L, MM = (size_t)n.M * n.M;
+    const size_t L = n.L, M = n.M, MM = M * M;
     for (size_t k = 0; k < (size_t)cnt * L; ++k) sneed(types[k] <= 1, "bead type must be 0 (A) or 1 (B)");
-    std::vector<float> t((size_t)cnt * MM);
-    double mean = 0;
-    for (size_t k = 0; k < t.size(); ++k) {
-      sneed(std::isfinite(maps[k]) && maps[k] >= 0.0f, "contact probabilities must be finite and >= 0");
-      t[k] = std::log(maps[k] + n.cfg.target_eps);
-      mean += t[k];
+    double total = 0;
+    std::vector<double> ps(M, 0.0);
+    for (size_t k = 0; k < (size_t)cnt * MM; ++k) {
+      sneed(std::isfinite(maps[k]) && maps[k] >= 0.0f && maps[k] <= 1.0f,
+            "contact probabilities must be finite and in [0, 1]");
+      const size_t r = k % MM, i = r / M, j = r % M;
+      ps[i > j ? i - j : j - i] += maps[k];
+      total += maps[k];
+    }
+    // separation weights: w[s] = M / (mean P(s) x bin pairs at separation s),
+    // so every separation carries the same total weight (relative to its
+    // contact probability); the mean over all pixels of w[s] P(s) is 1
+    std::vector<float> sw(M);
+    for (size_t s = 0; s < M; ++s) {
+      const double npairs = (double)(s == 0 ? M : 2 * (M - s));
+      sw[s] = (float)((double)M / (std::max(ps[s] / ((double)cnt * npairs), 1e-6) * npairs));
     }
     std::vector<uint8_t> lf((size_t)cnt * L, 0);
     if (lad)
@@ -858,12 +886,14 @@ int ccpsur_set_dataset(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, 
     n.ds_types.alloc((size_t)cnt * L);
     n.ds_lad.alloc((size_t)cnt * L);
     n.ds_target.alloc((size_t)cnt * MM);
+    n.ds_sweight.alloc(M);
     SCK(cudaMemcpyAsync(n.ds_types.p, types, (size_t)cnt * L, cudaMemcpyHostToDevice, n.st));
     SCK(cudaMemcpyAsync(n.ds_lad.p, lf.data(), lf.size(), cudaMemcpyHostToDevice, n.st));
-    SCK(cudaMemcpyAsync(n.ds_target.p, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, n.st));
+    SCK(cudaMemcpyAsync(n.ds_target.p, maps, sizeof(float) * (size_t)cnt * MM, cudaMemcpyHostToDevice, n.st));
+    SCK(cudaMemcpyAsync(n.ds_sweight.p, sw.data(), sizeof(float) * M, cudaMemcpyHostToDevice, n.st));
     n.ds_n = cnt;
-    if (n.step == 0) {  // start the output bias at the mean target
-      const float bo = (float)(mean / (double)t.size());
+    if (n.step == 0) {  // start the output bias at the log of the mean contact probability
+      const float bo = (float)std::log(std::max(total / ((double)cnt * MM), 1e-6));
       SCK(cudaMemcpyAsync(n.params.p + n.bo_off, &bo, sizeof(float), cudaMemcpyHostToDevice, n.st));
     }
     SCK(cudaStreamSynchronize(n.st));

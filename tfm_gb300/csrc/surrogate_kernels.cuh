@@ -653,27 +653,38 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Prediction: symmetrised log map -> contact probability max(exp(yhat) - eps, 0).
-__global__ void k_predict_maps(const float *__restrict__ y, int M, int n, float eps, float *__restrict__ out) {
+// The network predicts log contact probabilities; yhat = (y + y^T) / 2 is
+// clamped to YHAT_MAX = 0 (probability 1) before exponentiation. The loss
+// gradient is taken at the clamped value and passed through unchanged
+// (straight-through), so a prediction above 1 is pulled back down.
+constexpr float YHAT_MAX = 0.0f;
+
+// Prediction: contact probability exp(yhat).
+__global__ void k_predict_maps(const float *__restrict__ y, int M, int n, float *__restrict__ out) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long long)n * M * M) return;
   const long long b = k / ((long long)M * M);
   const int r = (int)(k - b * M * M), i = r / M, j = r - i * M;
   const float yh = 0.5f * (y[k] + y[b * M * M + (long long)j * M + i]);
-  out[k] = fmaxf(expf(yh) - eps, 0.0f);
+  out[k] = expf(fminf(yh, YHAT_MAX));
 }
 
-// Loss and the gradient entering the head. yhat = (y + y^T) / 2, loss =
-// mean (yhat - t)^2 over n M^2 values (targets symmetric, so dL/dy = dL/dyhat).
+// Loss and the gradient entering the head. yhat = (y + y^T) / 2 and the
+// Poisson deviance of the observed contact probability p against exp(yhat),
+// weighted per separation s = |i - j| by w[s] (the inverse of the dataset's
+// mean P(s)), averaged over n M^2 values:
+//   loss = mean w[s] (exp(yhat) - p - p (yhat - log p)),
+//   dL/dyhat = w[s] (exp(yhat) - p) / (n M^2).
+// Targets are symmetric, so dL/dy = dL/dyhat.
 // The gradient of the last head output is the rank-1 dz[p][c] = dy[p] wo[c]:
 // only dy is stored (the next convolution's epilogue expands it); dc[p][c] =
 // dz masked by the last head layer's ReLU bits (BF16). Accumulates d wo,
 // d bo and the loss.
 __global__ void __launch_bounds__(256)
-    k_loss_out_bwd(const float *__restrict__ y, const float *__restrict__ target, const int32_t *__restrict__ idx,
-                   const bf16 *__restrict__ z, const uint32_t *__restrict__ mask, const float *__restrict__ wo,
-                   int M, int n, float *__restrict__ dy, bf16 *__restrict__ dc, float *__restrict__ gwo,
-                   float *__restrict__ gbo, double *__restrict__ loss) {
+    k_loss_out_bwd(const float *__restrict__ y, const float *__restrict__ target, const float *__restrict__ sw,
+                   const int32_t *__restrict__ idx, const bf16 *__restrict__ z, const uint32_t *__restrict__ mask,
+                   const float *__restrict__ wo, int M, int n, float *__restrict__ dy, bf16 *__restrict__ dc,
+                   float *__restrict__ gwo, float *__restrict__ gbo, double *__restrict__ loss) {
   __shared__ float swo[64];
   __shared__ float red[8][65];
   if (threadIdx.x < 64) swo[threadIdx.x] = wo[threadIdx.x];
@@ -688,11 +699,13 @@ __global__ void __launch_bounds__(256)
   if (p < P) {
     const long long b = p / MM;
     const int r = (int)(p - b * MM), i = r / M, j = r - i * M;
-    const float yh = 0.5f * (y[p] + y[b * MM + (long long)j * M + i]);
+    const float yh = fminf(0.5f * (y[p] + y[b * MM + (long long)j * M + i]), YHAT_MAX);
     const long long row = idx ? idx[b] : b;
-    const float d = yh - target[row * MM + r];
-    l2 = d * d;
-    dyv = 2.0f * d / (float)P;
+    const float t = target[row * MM + r];
+    const float w = sw[abs(i - j)];
+    const float e = expf(yh);
+    l2 = w * (e - t - (t > 0.0f ? t * (yh - logf(t)) : 0.0f));
+    dyv = w * (e - t) / (float)P;
     dy[p] = dyv;
     const uint32_t m0 = mask[p * 2], m1 = mask[p * 2 + 1];
     for (int c0 = 0; c0 < 64; c0 += 16) {
@@ -824,13 +837,38 @@ __global__ void k_unpool(const float *__restrict__ dhp, const uint32_t *__restri
   store_bf16x16(dc + bl * 128 + c0, v);
 }
 
+// Sum of squared gradients (FP64) for the global-norm clip.
+__global__ void __launch_bounds__(256) k_grad_sq(const float *__restrict__ g, long long n, double *__restrict__ out) {
+  double s = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    s += (double)g[k] * g[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double r[8];
+  if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += r[w];
+    atomicAdd(out, t);
+  }
+}
+
 // AdamW over the whole FP32 parameter vector; decay[k] selects weight decay.
+// The gradient is scaled by min(1, clip / ||g||) when clip > 0 (gsq: the
+// squared norm from k_grad_sq).
 __global__ void k_adamw(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
                         float *__restrict__ v, const uint8_t *__restrict__ decay, long long n, float lr, float b1,
-                        float b2, float eps, float wd, float bc1, float bc2) {
+                        float b2, float eps, float wd, float bc1, float bc2, float clip,
+                        const double *__restrict__ gsq) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const float gk = g[k];
+  float scale = 1.0f;
+  if (clip > 0.0f) {
+    const double norm = sqrt(*gsq);
+    if (norm > clip) scale = (float)(clip / norm);
+  }
+  const float gk = g[k] * scale;
   const float mk = b1 * m[k] + (1.0f - b1) * gk;
   const float vk = b2 * v[k] + (1.0f - b2) * gk * gk;
   m[k] = mk;

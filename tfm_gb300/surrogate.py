@@ -302,10 +302,103 @@ def ps_curve(maps):
     return out
 
 
-def ps_error(pred, ref, s_min=1, s_max=None):
-    """Per map: mean over s in [s_min, s_max) of |P_pred(s) - P_ref(s)| / P_ref(s)."""
-    pp, pr = ps_curve(pred), ps_curve(ref)
-    M = pr.shape[1]
-    s_max = s_max or M // 2
-    rel = np.abs(pp[:, s_min:s_max] - pr[:, s_min:s_max]) / np.maximum(pr[:, s_min:s_max], 1e-12)
-    return rel.mean(axis=1)
+def ps_log_bins(maps):
+    """P(s) averaged over octaves of separation, s in [1, 2), [2, 4), ...,
+    [bins/4, bins/2): one value per octave and map."""
+    ps = ps_curve(maps)
+    M = ps.shape[1]
+    out, a = [], 1
+    while a < M // 2:
+        b = min(2 * a, M // 2)
+        out.append(ps[:, a:b].mean(axis=1))
+        a = b
+    return np.stack(out, axis=1)
+
+
+def ps_error(pred, ref):
+    """Per map: mean over separation octaves of |P_pred - P_ref| / P_ref."""
+    pp, pr = ps_log_bins(pred), ps_log_bins(ref)
+    return (np.abs(pp - pr) / np.maximum(pr, 1e-12)).mean(axis=1)
+
+
+def map_log_error(pred, ref, eps=1e-3):
+    """Per map: mean |log10(p_pred + eps) - log10(p_ref + eps)| over bin pairs."""
+    return np.abs(np.log10(np.asarray(pred, np.float64) + eps)
+                  - np.log10(np.asarray(ref, np.float64) + eps)).mean(axis=(1, 2))
+
+
+# ---------------------------------------------------------------- training and screening
+
+def train(net, n_train, epochs, seed, eval_rows=None):
+    """AdamW epochs over dataset rows [0, n_train) in seeded random batches of
+    the network's batch size. Returns per epoch the loss of one training
+    batch and, with eval_rows, the mean loss over those rows."""
+    B = net.info().batch
+    rng = np.random.default_rng(seed)
+    history = []
+    for ep in range(epochs):
+        perm = rng.permutation(n_train).astype(np.int32)
+        for i in range(max(1, n_train // B)):
+            net.train_step(perm[i * B:(i + 1) * B], want_loss=False)
+        rec = {"epoch": ep + 1, "train_loss": net.loss_grad(perm[:B])}
+        if eval_rows is not None and len(eval_rows) >= B:
+            ev = np.asarray(eval_rows, np.int32)
+            rec["heldout_loss"] = float(np.mean([net.loss_grad(ev[i:i + B])
+                                                 for i in range(0, len(ev) - B + 1, B)]))
+        history.append(rec)
+    return history
+
+
+def envelope(maps, margin=0.25):
+    """Per separation octave, the range of P(s) over a set of maps widened by
+    `margin` (relative) on both sides: where a prediction may fall without
+    being re-simulated."""
+    pb = ps_log_bins(maps)
+    return pb.min(axis=0) * (1.0 - margin), pb.max(axis=0) * (1.0 + margin)
+
+
+def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
+    """Batched inference over many sequences with a simulation fallback: a
+    random `fallback_fraction` of them, plus every sequence whose predicted
+    P(s) leaves the envelope in some separation octave, is re-simulated by
+    `sim` (a callable (types, lad) -> maps), which judges the prediction.
+    Returns a report and the indices re-simulated."""
+    import time
+
+    n = types.shape[0]
+    rng = np.random.default_rng(seed)
+    lo, hi = env
+    out_env = np.zeros(n, bool)
+    pb_pred = None
+    t0 = time.perf_counter()
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        pb = ps_log_bins(net.predict(types[a:b], lad[a:b]))
+        if pb_pred is None:
+            pb_pred = np.empty((n, pb.shape[1]))
+        pb_pred[a:b] = pb
+        out_env[a:b] = np.any((pb < lo) | (pb > hi), axis=1)
+    t_pred = time.perf_counter() - t0
+    k = max(1, int(round(fallback_fraction * n)))
+    rand = rng.choice(n, k, replace=False)
+    fb = np.union1d(rand, np.nonzero(out_env)[0])
+    t1 = time.perf_counter()
+    sim_maps = sim(types[fb], lad[fb])
+    t_sim = time.perf_counter() - t1
+    pb_sim = ps_log_bins(sim_maps)
+    err = (np.abs(pb_pred[fb] - pb_sim) / np.maximum(pb_sim, 1e-12)).mean(axis=1)
+    in_rand = np.isin(fb, rand)
+    rep = {
+        "sequences": int(n),
+        "predict_s": t_pred,
+        "maps_per_s_with_host_io": n / t_pred,
+        "fallback_random": int(k),
+        "fallback_out_of_envelope": int(out_env.sum()),
+        "simulated": int(len(fb)),
+        "simulate_s": t_sim,
+        "ps_error_random_sample": {"mean": float(err[in_rand].mean()), "median": float(np.median(err[in_rand])),
+                                   "p90": float(np.percentile(err[in_rand], 90))},
+    }
+    if (~in_rand).any():
+        rep["ps_error_out_of_envelope"] = float(err[~in_rand].mean())
+    return rep, fb
