@@ -1,4 +1,5 @@
-"""Benchmark of the BD engine: bead-steps/s of the batched replica ensemble.
+"""Benchmark of the BD engine: bead-steps/s of the batched replica ensemble,
+and of the contact-map surrogate trained on the engine's maps.
 
 Workload: 512 independent replicas with bead counts N_i = floor(exp(U(ln 1024,
 ln 16384))) (seeded), each with its own seeded two-state Markov type sequence
@@ -14,7 +15,14 @@ state resident in HBM (CUDA events on the engine's stream); `e2e` = the same
 through the C ABI with host buffers (positions uploaded from host memory and
 downloaded after every bench step). The state (~280 MB) is larger than L2.
 
+The default run adds a `surrogate` block: 512 sequences simulated, the network
+trained on 90 % of them and scored on the rest, batched inference timed.
+`--surrogate` runs the full surrogate protocol instead (4096 training
+sequences, 10^5 screened with a 1 % simulation fallback) and prints its own line.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+  python bench.py --surrogate [--sur-sequences 4096] [--sur-sim-steps 20000]
+                  [--sur-epochs 30] [--sur-screen 100000] [--sim-rate BEAD_STEPS_PER_S]
 """
 import argparse
 import json
@@ -295,6 +303,9 @@ def engine_arm(args, ws, rank, local):
     extras = {}
     if rank == 0 and not args.no_extras:
         extras = measure_extras(args, sizes, b)
+        b.close()
+        extras["surrogate"] = surrogate_report(value / ws, n_seq=512, sim_steps=10000, epochs=15,
+                                               judge_reps=2, screen_n=0)
 
     if rank == 0:
         line = {
@@ -390,6 +401,154 @@ def measure_extras(args, sizes, b):
     return out
 
 
+# ---------------------------------------------------------------- surrogate
+
+SUR_L, SUR_M = 1024, 256
+# forward FLOPs of one map: 6 head 3x3 convolutions 64 -> 64 at bins^2 pixels,
+# the 8 encoder convolutions (kernel 5) at seq_len positions, the projection
+SUR_FWD_FLOP = (6 * 2 * SUR_M * SUR_M * 9 * 64 * 64 + 2 * SUR_L * 5 * 64 * 128
+                + 7 * 2 * SUR_L * 5 * 128 * 128 + 2 * SUR_M * 128 * 128)
+SIM_STEPS_PER_MAP = 100000  # the batched-ensemble protocol: 1e5 Heun steps per map
+
+
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, judge_reps, screen_n, seed=7):
+    """Simulate contact maps of n_seq seeded sequences (1024 beads, 256 bins)
+    with the batched engine, train the surrogate on 90 % of them with its own
+    tensor-core kernels, score the held-out 10 % (P(s) error per separation
+    octave against the simulation, against the mean of `judge_reps` fresh
+    replica simulations, and the same numbers for a second simulation and for
+    the training set's mean map), time batched inference with the inputs on
+    the device and through the C ABI with host buffers, and optionally screen
+    `screen_n` new sequences with a 1 % + out-of-envelope simulation fallback."""
+    import torch
+
+    from tfm_gb300 import surrogate as S
+
+    t0 = time.perf_counter()
+    types, lad, _ = S.make_sequences(n_seq, SUR_L, seed)
+    burn, every = 2000, 100
+    maps, frames = S.simulate_maps(types, lad, SUR_M, sim_steps, burn, every, seed=100)
+    t_sim = time.perf_counter() - t0
+    nh = max(32, n_seq // 10)
+    ntr = n_seq - nh
+    held = np.arange(ntr, n_seq, dtype=np.int32)
+    k = min(64, nh)
+    reps = [S.simulate_maps(types[ntr:ntr + k], lad[ntr:ntr + k], SUR_M, sim_steps, burn, every,
+                            seed=1000 + 17 * r)[0] for r in range(judge_reps)]
+    judge = np.mean(reps, axis=0)
+    mean_map = maps[:ntr].mean(axis=0, keepdims=True)
+    B = 32
+    steps_total = epochs * max(1, ntr // B)
+    net = S.Surrogate("batch %d\nlr 1e-3\nlr_min 1e-4\nlr_steps %d\n" % (B, steps_total), seed=3)
+    net.set_dataset(types, lad, maps)
+    t1 = time.perf_counter()
+    hist = S.train(net, ntr, epochs, seed=5, eval_rows=held)
+    t_train = time.perf_counter() - t1
+    pred = net.predict_rows(held)
+    e = S.ps_error(pred, maps[ntr:])
+    rep = {
+        "workload": "c3: %d seeded two-type sequences of 1024 beads (Markov block length U[4, 64], "
+                    "10%% LAD), 256^2 contact-probability maps from the batched engine "
+                    "(%d + %d Heun steps, %d frames), 10%% held out" % (n_seq, burn, sim_steps, frames),
+        "simulate_s": t_sim, "train_s": t_train, "epochs": epochs, "optimizer_steps": steps_total,
+        "heldout_loss": hist[-1].get("heldout_loss"),
+        "ps_error": {"vs_simulation": float(e.mean()),
+                     "vs_mean_of_%d_replicas" % judge_reps: float(S.ps_error(pred[:k], judge).mean()),
+                     "metric": "mean over separation octaves [1,2)..[64,128) of |P_pred - P_sim| / P_sim"},
+        "baselines": {
+            "second_simulation_vs_simulation": float(S.ps_error(reps[0], maps[ntr:ntr + k]).mean()),
+            "second_simulation_vs_mean_of_others": float(S.ps_error(
+                reps[0], np.mean(reps[1:], axis=0)).mean()) if judge_reps > 2 else None,
+            "training_mean_map_vs_simulation": float(S.ps_error(np.repeat(mean_map, nh, 0), maps[ntr:]).mean()),
+            "training_mean_map_vs_mean_of_replicas": float(S.ps_error(np.repeat(mean_map, k, 0), judge).mean()),
+        },
+        # per bin pair, against the replica mean (one run is mostly zero counts far
+        # from the diagonal, which an expected-probability predictor cannot match)
+        "map_log10_mae_vs_mean_of_replicas": {
+            "surrogate": float(S.map_log_error(pred[:k], judge).mean()),
+            "one_simulation": float(S.map_log_error(maps[ntr:ntr + k], judge).mean()),
+            "training_mean_map": float(S.map_log_error(np.repeat(mean_map, k, 0), judge).mean())},
+    }
+    # inference throughput, inputs resident: batches of dataset rows
+    st = torch.cuda.ExternalStream(net.stream())
+    rows = np.arange(n_seq, dtype=np.int32)
+    nb = 64
+    for i in range(3):
+        net.predict_rows(rows[(i * B) % n_seq:(i * B) % n_seq + B], copy=False)
+    net.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    k0 = net.kernel_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for i in range(nb):
+        a = (i * B) % (n_seq - B + 1)
+        net.predict_rows(rows[a:a + B], copy=False)
+    e1.record(st)
+    net.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    maps_s = nb * B / (ms / 1000.0)
+    peak, kind = bf16_peak()
+    tflops = maps_s * SUR_FWD_FLOP / 1e12
+    sim_maps_s = bead_steps_per_s / (SUR_L * SIM_STEPS_PER_MAP)
+    # end to end: host sequences in, host maps out
+    tt, tl = types[:256], lad[:256]
+    net.predict(tt[:B], tl[:B])
+    t2 = time.perf_counter()
+    net.predict(tt, tl)
+    e2e = 256 / (time.perf_counter() - t2)
+    rep.update({
+        "maps_per_s": maps_s, "ms_per_batch_of_32": ms / nb, "gpu_launches_per_batch": (net.kernel_count() - k0) / nb,
+        "clocks": clk,
+        "roofline": {"bound": "tensor", "kernel": "forward pass (head 3x3 convolutions dominate)",
+                     "achieved": tflops, "peak": peak, "peak_kind": kind, "unit": "TFLOP/s",
+                     "frac": tflops / peak, "gflop_per_map": SUR_FWD_FLOP / 1e9},
+        "e2e_maps_per_s": e2e,
+        "simulated_maps_per_s": sim_maps_s,
+        "speedup_vs_simulation": maps_s / sim_maps_s,
+        "speedup_basis": "simulation of one 1024-bead map for %d Heun steps at the batched engine's "
+                         "measured bead-steps/s" % SIM_STEPS_PER_MAP,
+    })
+    if screen_n:
+        env = S.envelope(maps[:ntr])
+        sim = lambda t, l: S.simulate_maps(t, l, SUR_M, sim_steps, burn, every, seed=5000)[0]
+        stypes, slad, _ = S.make_sequences(screen_n, SUR_L, seed + 1)
+        srep, _ = S.screen(net, stypes, slad, env, 0.01, seed=11, sim=sim)
+        rep["screening"] = dict(srep, workload="c4: %d new seeded sequences, 1%% random + "
+                                               "out-of-envelope re-simulated" % screen_n)
+    rep["error_flags"] = net.error_flags()
+    net.close()
+    return rep
+
+
+def surrogate_arm(args, rank, local):
+    import torch
+
+    from tfm_gb300 import build as eb
+
+    eb.build()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    rep = surrogate_report(args.sim_rate, args.sur_sequences, args.sur_sim_steps, args.sur_epochs, 4,
+                           args.sur_screen)
+    line = {"metric": "surrogate contact maps/s (batched BF16 inference, 1 GB300)", "value": rep["maps_per_s"],
+            "unit": "maps/s", "n_gpus": 1, "higher_is_better": True, "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic (seeded sequences, maps simulated by the engine)",
+            "config": {"workload": rep["workload"]}}
+    line.update({k: v for k, v in rep.items() if k not in ("maps_per_s", "workload")})
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,9 +558,19 @@ def main():
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
+    ap.add_argument("--surrogate", action="store_true",
+                    help="measure the surrogate on the c3/c4 protocol instead of the engine")
+    ap.add_argument("--sur-sequences", type=int, default=4096)
+    ap.add_argument("--sur-sim-steps", type=int, default=20000)
+    ap.add_argument("--sur-epochs", type=int, default=30)
+    ap.add_argument("--sur-screen", type=int, default=100000)
+    ap.add_argument("--sim-rate", type=float, default=1.9e9,
+                    help="batched bead-steps/s used to cost a simulated map (from the engine bench)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.surrogate:
+        surrogate_arm(args, rank, local)
+    elif args.impl == "reference":
         reference_arm(args, ws, rank)
     else:
         engine_arm(args, ws, rank, local)
