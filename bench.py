@@ -15,7 +15,7 @@ state resident in HBM (CUDA events on the engine's stream); `e2e` = the same
 through the C ABI with host buffers (positions uploaded from host memory and
 downloaded after every bench step). The state (~280 MB) is larger than L2.
 
-The default run adds a `surrogate` block: 512 sequences simulated, the network
+The default run adds a `surrogate` block: 1024 sequences simulated, the network
 trained on 90 % of them and scored on the rest, batched inference timed.
 `--surrogate` runs the full surrogate protocol instead (4096 training
 sequences, 10^5 screened with a 1 % simulation fallback) and prints its own line.
@@ -304,8 +304,8 @@ def engine_arm(args, ws, rank, local):
     if rank == 0 and not args.no_extras:
         extras = measure_extras(args, sizes, b)
         b.close()
-        extras["surrogate"] = surrogate_report(value / ws, n_seq=512, sim_steps=10000, epochs=15,
-                                               judge_reps=2, screen_n=0)
+        extras["surrogate"] = surrogate_report(value / ws, n_seq=1024, sim_steps=10000, epochs=30,
+                                               judge_reps=3, screen_n=0)
 
     if rank == 0:
         line = {

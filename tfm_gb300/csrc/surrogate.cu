@@ -379,7 +379,16 @@ struct Net {
   int ds_n = 0;
   Buf<int32_t> d_rows;
   Buf<uint8_t> in_types, in_lad;
-  int32_t *h_rows = nullptr;  // pinned staging for row indices
+  int32_t *h_rows = nullptr;  // pinned staging for row indices: two slots of `batch`
+  cudaEvent_t ev_rows[2] = {nullptr, nullptr};
+  int rows_slot = 0;
+  // pinned staging of predicted maps: two slots of `batch` maps, drained into
+  // the caller's buffer while the next batch runs
+  float *h_maps = nullptr;
+  cudaEvent_t ev_maps[2] = {nullptr, nullptr};
+  float *pend_dst[2] = {nullptr, nullptr};
+  size_t pend_n[2] = {0, 0};
+  int maps_slot = 0;
   cudaStream_t st = nullptr;
   Launcher run;
 
@@ -459,13 +468,23 @@ struct Net {
     d_rows.alloc(c.batch);
     in_types.alloc((size_t)c.batch * L);
     in_lad.alloc((size_t)c.batch * L);
-    SCK(cudaMallocHost(&h_rows, sizeof(int32_t) * c.batch));
+    SCK(cudaMallocHost(&h_rows, sizeof(int32_t) * 2 * c.batch));
+    SCK(cudaMallocHost(&h_maps, sizeof(float) * 2 * (size_t)c.batch * M * M));
+    for (int k = 0; k < 2; ++k) {
+      SCK(cudaEventCreateWithFlags(&ev_rows[k], cudaEventDisableTiming));
+      SCK(cudaEventCreateWithFlags(&ev_maps[k], cudaEventDisableTiming));
+    }
     SCK(cudaStreamSynchronize(st));
   }
 
   ~Net() {
     if (st) cudaStreamSynchronize(st);
     if (h_rows) cudaFreeHost(h_rows);
+    if (h_maps) cudaFreeHost(h_maps);
+    for (int k = 0; k < 2; ++k) {
+      if (ev_rows[k]) cudaEventDestroy(ev_rows[k]);
+      if (ev_maps[k]) cudaEventDestroy(ev_maps[k]);
+    }
     if (st) cudaStreamDestroy(st);
   }
 
@@ -718,12 +737,16 @@ struct Net {
   const int32_t *upload_rows(const int32_t *rows, int n) {
     if (n < 1 || n > cfg.batch) throw Error(ST_ARG, "row count must be in [1, batch]");
     if (ds_n == 0) throw Error(ST_STATE, "no dataset");
-    SCK(cudaStreamSynchronize(st));  // the pinned staging buffer may still be in use
+    // alternate pinned slots; wait only for the copy that last read this slot
+    rows_slot ^= 1;
+    int32_t *hr = h_rows + (size_t)rows_slot * cfg.batch;
+    SCK(cudaEventSynchronize(ev_rows[rows_slot]));
     for (int i = 0; i < n; ++i) {
       if (rows[i] < 0 || rows[i] >= ds_n) throw Error(ST_ARG, "dataset row out of range");
-      h_rows[i] = rows[i];
+      hr[i] = rows[i];
     }
-    SCK(cudaMemcpyAsync(d_rows.p, h_rows, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    SCK(cudaMemcpyAsync(d_rows.p, hr, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    SCK(cudaEventRecord(ev_rows[rows_slot], st));
     return d_rows.p;
   }
 
@@ -750,13 +773,38 @@ struct Net {
     return l;
   }
 
+  // Maps of the last forward pass: to the device buffer `pred`, and with
+  // maps_host through a pinned slot into maps_host[first ...]; the slot is
+  // copied out by drain_maps while later batches run.
   void predict_out(int n, float *maps_host, size_t first) {
     const long long P = (long long)n * M * M;
     k_predict_maps<<<blocks(P), 256, 0, st>>>(y.p, M, n, pred.p);
     SCK(cudaGetLastError());
     ++run.kernels;
-    if (maps_host)
-      SCK(cudaMemcpyAsync(maps_host + first * (size_t)M * M, pred.p, sizeof(float) * P, cudaMemcpyDeviceToHost, st));
+    if (!maps_host) return;
+    maps_slot ^= 1;
+    drain_slot(maps_slot);
+    float *stage = h_maps + (size_t)maps_slot * cfg.batch * M * M;
+    SCK(cudaMemcpyAsync(stage, pred.p, sizeof(float) * P, cudaMemcpyDeviceToHost, st));
+    SCK(cudaEventRecord(ev_maps[maps_slot], st));
+    pend_dst[maps_slot] = maps_host + first * (size_t)M * M;
+    pend_n[maps_slot] = (size_t)P;
+    drain_slot(maps_slot ^ 1);
+  }
+
+  void drain_slot(int k) {
+    if (!pend_dst[k]) return;
+    SCK(cudaEventSynchronize(ev_maps[k]));
+    std::memcpy(pend_dst[k], h_maps + (size_t)k * cfg.batch * M * M, sizeof(float) * pend_n[k]);
+    pend_dst[k] = nullptr;
+  }
+
+  // forget copies owed to an earlier call that failed part-way
+  void discard_pending() { pend_dst[0] = pend_dst[1] = nullptr; }
+
+  void drain_maps() {
+    drain_slot(maps_slot ^ 1);
+    drain_slot(maps_slot);
   }
 };
 
@@ -923,16 +971,17 @@ int ccpsur_predict(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int3
     Net &n = net_of(h);
     sneed(types && maps && cnt >= 0, "null argument");
     const size_t L = n.L;
-    std::vector<uint8_t> lf;
+    n.discard_pending();
     for (int32_t first = 0; first < cnt; first += n.cfg.batch) {
       const int b = std::min(n.cfg.batch, cnt - first);
-      SCK(cudaStreamSynchronize(n.st));
+      // pageable sources: the copies return once the data is staged
       SCK(cudaMemcpyAsync(n.in_types.p, types + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
       if (lad)
         SCK(cudaMemcpyAsync(n.in_lad.p, lad + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
       n.forward(n.in_types.p, lad ? n.in_lad.p : nullptr, nullptr, b, false);
       n.predict_out(b, maps, first);
     }
+    n.drain_maps();
     n.check_flags();
   });
 }
@@ -941,13 +990,17 @@ int ccpsur_predict_rows(ccpsur_net *h, const int32_t *rows, int32_t cnt, float *
   return sguard([&] {
     Net &n = net_of(h);
     sneed(rows && cnt >= 0, "null argument");
+    n.discard_pending();
     for (int32_t first = 0; first < cnt; first += n.cfg.batch) {
       const int b = std::min(n.cfg.batch, cnt - first);
       const int32_t *r = n.upload_rows(rows + first, b);
       n.forward(n.ds_types.p, n.ds_lad.p, r, b, false);
       n.predict_out(b, maps, first);
     }
-    if (maps) n.check_flags();
+    if (maps) {
+      n.drain_maps();
+      n.check_flags();
+    }
   });
 }
 
