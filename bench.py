@@ -530,6 +530,28 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, judge_reps, scr
     return rep
 
 
+def surrogate_profile_case():
+    """A small surrogate workload for profiler captures: batch 16 of the
+    default network (1024 beads, 256 bins), two batched predictions and one
+    training step on a synthetic dataset."""
+    from tfm_gb300 import surrogate as S
+
+    net = S.Surrogate("batch 16\n", seed=1)
+    types, lad, _ = S.make_sequences(16, SUR_L, 1)
+    i = np.arange(SUR_M)
+    base = (0.5 / (1.0 + np.abs(i[:, None] - i[None, :])) ** 1.1).astype(np.float32)
+    net.set_dataset(types, lad, np.repeat(base[None], 16, 0))
+    rows = np.arange(16, dtype=np.int32)
+    for _ in range(2):
+        net.predict_rows(rows, copy=False)
+    net.train_step(rows, want_loss=False)
+    net.synchronize()
+    if net.error_flags():
+        raise RuntimeError("surrogate kernels reported a pipeline timeout")
+    net.close()
+    print("surrogate profile case done")
+
+
 def surrogate_arm(args, rank, local):
     import torch
 
@@ -560,6 +582,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
     ap.add_argument("--surrogate", action="store_true",
                     help="measure the surrogate on the c3/c4 protocol instead of the engine")
+    ap.add_argument("--sur-profile", action="store_true",
+                    help="run only a small surrogate workload (for profiler captures)")
     ap.add_argument("--sur-sequences", type=int, default=4096)
     ap.add_argument("--sur-sim-steps", type=int, default=20000)
     ap.add_argument("--sur-epochs", type=int, default=30)
@@ -568,7 +592,12 @@ def main():
                     help="batched bead-steps/s used to cost a simulated map (from the engine bench)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
-    if args.surrogate:
+    if args.sur_profile:
+        from tfm_gb300 import build as eb
+
+        eb.build()
+        surrogate_profile_case()
+    elif args.surrogate:
         surrogate_arm(args, rank, local)
     elif args.impl == "reference":
         reference_arm(args, ws, rank)
