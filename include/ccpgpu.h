@@ -214,6 +214,43 @@ int ccpgpu_separation_counts(ccpgpu_sim *h, int32_t chain, int32_t *counts, doub
  * (chrsim::particle_overlaps, chrsim.cu:805-820). */
 int ccpgpu_overlaps(ccpgpu_sim *h, uint64_t *per_system, size_t n);
 
+/* ---------------------------------------------------------------- analysis */
+
+/* ccp-analyze's outputs (Program/src/ccp-analyze.cu:52-126), fed by the GPU
+ * observables instead of re-read trajectory files. A simulation is what one
+ * system runs between two ccpgpu_analysis_end_simulation calls (ccp-analyze:
+ * one initial condition and its trajectories); in a batch each system is a
+ * simulation. The frames share the observable buffers of ccpgpu_observe, so
+ * do not observe otherwise (ccpgpu_observe, observe_every) during one. */
+
+/* One frame of every system at the current positions (chrana::
+ * calc_observables, chrana.cu:371-512): centre-of-mass distance, gyration
+ * radius squared, nematic order parameter, nucleus chromatin fraction and
+ * radial chromatin density join each system's time series; contact map,
+ * contact probability and spatial distance by separation accumulate. */
+int ccpgpu_analysis_frame(ccpgpu_sim *h);
+/* The time series of system sys's current simulation: frames = its frame
+ * count; with out, series k (0 dcm, 1 rg2, 2 nop, 3 ncf, 4 + t*64 + b the
+ * radial density of type t = A, B, all in shell b) in out[k * frames ...].
+ * n: capacity of out in floats. */
+int ccpgpu_analysis_series(ccpgpu_sim *h, int32_t sys, float *out, size_t n, int32_t *frames);
+/* Ends every system's simulation (calc_last_is_stat, clear_is_var,
+ * chrana.cu:177-305): statistics of the series (sostat.cu:136-174:
+ * thermalisation by the marginal standard error rule, standard error by
+ * blocking), frame averages of the rest, and adds them to the combined
+ * statistics. Clears the observable buffers. */
+int ccpgpu_analysis_end_simulation(ccpgpu_sim *h);
+/* analysis-XXX.dat of system sys's last simulation (save_last_is_stat,
+ * chrana.cu:205-256): the byte image ccp-analyze writes. */
+int ccpgpu_analysis_txt(ccpgpu_sim *h, int32_t sys, char *buf, size_t cap, size_t *len);
+/* analysis-fin.dat over every simulation so far (calc_cs_final_stat +
+ * save_cs_final_stat, chrana.cu:281-360, sostat.cu:176-224). The systems must
+ * share size, chains, contact bins and radius. */
+int ccpgpu_analysis_fin_txt(ccpgpu_sim *h, char *buf, size_t cap, size_t *len);
+/* contact-map.bin: the packed lower-triangular contact-map averages over
+ * every simulation so far as float64 (save_cm_avg_bin, chrana.cu:362-369). */
+int ccpgpu_contact_map_bin(ccpgpu_sim *h, char *buf, size_t cap, size_t *len);
+
 /* ---------------------------------------------------------------- no allocation */
 
 /* Total force of one system evaluated without allocating device memory. No

@@ -1,7 +1,7 @@
 """Builds libccpgpu.so (the engine's C-ABI library) in-tree for sm_103a.
 
-Three translation units (host C++, the CUDA engine and the surrogate
-network) are compiled in parallel with nvcc and linked into tfm_gb300/libccpgpu.so. No cmake.
+Four translation units (host C++, the analysis statistics, the CUDA engine
+and the surrogate network) are compiled in parallel with nvcc and linked into tfm_gb300/libccpgpu.so. No cmake.
 """
 import os
 import shutil
@@ -31,7 +31,7 @@ def _run(cmd):
 
 
 def sources():
-    return [os.path.join(CSRC, f) for f in ("host.cpp", "engine.cu", "surrogate.cu")]
+    return [os.path.join(CSRC, f) for f in ("host.cpp", "analysis.cpp", "engine.cu", "surrogate.cu")]
 
 
 def _stale(target, deps):

@@ -32,7 +32,9 @@ SYMBOLS = (
     "ccpgpu_reset_observables", "ccpgpu_contact_counts", "ccpgpu_observable_sums",
     "ccpgpu_separation_counts", "ccpgpu_overlaps", "ccpgpu_advance", "ccpgpu_synchronize",
     "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
-    "ccpgpu_forces_noalloc", "ccpgpu_autotune",
+    "ccpgpu_forces_noalloc", "ccpgpu_autotune", "ccpgpu_analysis_frame", "ccpgpu_analysis_series",
+    "ccpgpu_analysis_end_simulation", "ccpgpu_analysis_txt", "ccpgpu_analysis_fin_txt",
+    "ccpgpu_contact_map_bin",
 )
 
 NOALLOC_MAX_BEADS = 32768
@@ -117,6 +119,11 @@ def load(path=LIB_PATH):
         "ccpgpu_kernel_count": [P, C.POINTER(C.c_uint64)],
         "ccpgpu_forces_noalloc": [C.POINTER(NoallocSystem), P, P, P, P],
         "ccpgpu_autotune": [P, I32, P, SZ, C.POINTER(SZ)],
+        "ccpgpu_analysis_frame": [P], "ccpgpu_analysis_end_simulation": [P],
+        "ccpgpu_analysis_series": [P, I32, P, SZ, C.POINTER(I32)],
+        "ccpgpu_analysis_txt": [P, I32, P, SZ, C.POINTER(SZ)],
+        "ccpgpu_analysis_fin_txt": [P, P, SZ, C.POINTER(SZ)],
+        "ccpgpu_contact_map_bin": [P, P, SZ, C.POINTER(SZ)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -304,6 +311,42 @@ class _Handle:
     def load_checkpoint_bytes(self, b, s=0):
         buf = C.create_string_buffer(b, len(b))
         _check(_lib.ccpgpu_load_checkpoint(self._h, s, buf, len(b)))
+
+    # ---------------------------------------------------------------- analysis
+    def analysis_frame(self):
+        """One ccp-analyze frame of every system at the current positions."""
+        _check(_lib.ccpgpu_analysis_frame(self._h))
+
+    def analysis_series(self, s=0):
+        """Series [4 + 3*64][frames] of system s's current simulation."""
+        f = C.c_int32()
+        _check(_lib.ccpgpu_analysis_series(self._h, s, None, 0, C.byref(f)))
+        out = np.empty((4 + 3 * 64, f.value), np.float32)
+        _check(_lib.ccpgpu_analysis_series(self._h, s, _ptr(out), out.size, C.byref(f)))
+        return out
+
+    def analysis_end_simulation(self):
+        """Ends every system's simulation: statistics, then cleared buffers."""
+        _check(_lib.ccpgpu_analysis_end_simulation(self._h))
+
+    def analysis_txt(self, s=0):
+        """analysis-XXX.dat of system s's last simulation (bytes)."""
+        return self._bytes(_lib.ccpgpu_analysis_txt, s)
+
+    def _bytes0(self, fn):
+        n = C.c_size_t()
+        fn(self._h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        _check(fn(self._h, buf, n.value, C.byref(n)))
+        return buf.raw[: n.value]
+
+    def analysis_fin_txt(self):
+        """analysis-fin.dat over every simulation so far (bytes)."""
+        return self._bytes0(_lib.ccpgpu_analysis_fin_txt)
+
+    def contact_map_bin(self):
+        """contact-map.bin: float64 contact-map averages over simulations (bytes)."""
+        return self._bytes0(_lib.ccpgpu_contact_map_bin)
 
     def read_frame_txt_bytes(self, b, s=0):
         _check(_lib.ccpgpu_read_frame_txt(self._h, s, b, len(b)))

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/ccpgpu.h"
+#include "analysis.h"
 #include "host.h"
 #include "kernels.cuh"
 
@@ -91,6 +92,10 @@ struct Engine {
   DevBuf<int32_t> d_chain_of, d_chain_first, d_chain_len, d_chain_ps_off, d_chain_smax;
   DevBuf<int32_t> map, ps;
   DevBuf<double> obs, ds;
+  // ccp-analyze's outputs (analysis.h): per-frame sums of the observables and
+  // the nematic order / nucleus fraction sums of the frame being analysed
+  Analysis ana;
+  DevBuf<double> fobs, fextra;
   DevBuf<unsigned long long> ovl, d_step;
   DevBuf<int> d_err;
   DevBuf<float> xyz_stage;
@@ -777,6 +782,110 @@ struct Engine {
     frames_observed = 0;
   }
 
+  // One analysis frame of every system at the current positions
+  // (chrana::calc_observables, chrana.cu:371-512): the contact map, contact
+  // counts and distance sums by separation accumulate in the observable
+  // buffers shared with observe(); the per-frame scalars and radial densities
+  // are appended to each system's time series.
+  void analysis_frame() {
+    if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    const size_t ns = hsys.size();
+    if (ana.series.empty()) ana.resize((int)ns);
+    if (!fobs.p) {
+      fobs.alloc(ns * OBS_STRIDE);
+      fextra.alloc(ns * 2);
+    }
+    sort_now();
+    launch_observe_sorted(true);
+    CK(cudaMemsetAsync(fobs.p, 0, sizeof(double) * ns * OBS_STRIDE, stream));
+    CK(cudaMemsetAsync(fextra.p, 0, sizeof(double) * ns * 2, stream));
+    k_observe<<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, CCP_RCO / 2.0f, fobs.p);
+    k_frame_extra<<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, fextra.p);
+    kcount += 2;
+    recount();
+    CK(cudaGetLastError());
+    ++frames_observed;
+    std::vector<double> fo(ns * OBS_STRIDE), fx(ns * 2);
+    CK(cudaMemcpyAsync(fo.data(), fobs.p, sizeof(double) * fo.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(fx.data(), fextra.p, sizeof(double) * fx.size(), cudaMemcpyDeviceToHost, stream));
+    sync_and_check();
+    std::vector<float> v(ANA_SERIES);
+    for (size_t s = 0; s < ns; ++s) {
+      const SysDesc &d = hsys[s];
+      const double n = d.n;
+      const double *o = &fo[s * OBS_STRIDE];
+      const double cx = o[0] / n, cy = o[1] / n, cz = o[2] / n, c2 = cx * cx + cy * cy + cz * cz;
+      v[0] = (float)std::sqrt(c2);
+      v[1] = (float)(o[3] / n - c2);
+      v[2] = (float)(fx[2 * s] / (n - 1.0));
+      v[3] = (float)(fx[2 * s + 1] / n);
+      const double shell = (4.0 / 3.0) * 3.14159265358979323846 * (double)d.R_n * d.R_n * d.R_n / ANA_SHELLS;
+      for (int k = 0; k < 3 * ANA_SHELLS; ++k) v[4 + k] = (float)(o[4 + k] / shell);
+      ana.add_frame((int)s, v.data());
+    }
+  }
+
+  // Ends every system's simulation (calc_last_is_stat + clear_is_var,
+  // chrana.cu:177-305): frame-averaged spatial distance and contact
+  // probability by separation (calc_sd_cp, chrana.cu:13-45) per block and
+  // contact-map values (calc_cm, chrana.cu:48-84), statistics of the series,
+  // the analysis-XXX.dat text; then the observable buffers are cleared.
+  void analysis_end() {
+    const int frames = ana.series.empty() ? 0 : ana.frames(0);
+    if (frames == 0) throw Error(ST_STATE, "no analysis frame since the simulation began");
+    std::vector<int32_t> hmap(std::max<int64_t>(map_total, 1)), hps(std::max(ps_total, 1));
+    std::vector<double> hds(std::max(ps_total, 1));
+    CK(cudaMemcpyAsync(hmap.data(), map.p, sizeof(int32_t) * hmap.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hps.data(), ps.p, sizeof(int32_t) * hps.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(hds.data(), ds.p, sizeof(double) * hds.size(), cudaMemcpyDeviceToHost, stream));
+    sync_and_check();
+    for (size_t s = 0; s < hsys.size(); ++s) {
+      const SysDesc &d = hsys[s];
+      AnaLayout lay;
+      lay.n_beads = d.n;
+      lay.R_n = d.R_n;
+      // ccp's diploid model: one block per chromosome, both copies together;
+      // otherwise one block per chain (at least ccp's six)
+      const bool diploid = d.n_copies == 2 && d.n_chains == 12;
+      const int nblocks = diploid ? 6 : std::max(ANA_MIN_BLOCKS, d.n_chains);
+      lay.block_len.assign(nblocks, 0);
+      std::vector<std::vector<double>> sd(nblocks), cp(nblocks);
+      for (int blk = 0; blk < nblocks; ++blk) {
+        std::vector<int> chains;
+        if (diploid) chains = {d.chain_off + blk, d.chain_off + blk + 6};
+        else if (blk < d.n_chains) chains = {d.chain_off + blk};
+        if (chains.empty()) continue;
+        const int L = chain_len[chains[0]], rows = chain_smax[chains[0]];
+        lay.block_len[blk] = rows;
+        sd[blk].resize(rows);
+        cp[blk].resize(rows);
+        for (int sep = 1; sep <= rows; ++sep) {
+          double cnt = 0.0, dsum = 0.0;
+          for (int c : chains) {
+            cnt += hps[chain_ps_off[c] + sep];
+            dsum += hds[chain_ps_off[c] + sep];
+          }
+          const double denom = (double)frames * chains.size() * (L - sep);
+          cp[blk][sep - 1] = 1000.0 * cnt / denom;
+          sd[blk][sep - 1] = dsum / denom;
+        }
+      }
+      const int nb = d.nbins;
+      lay.cm_len = (int64_t)nb * (nb + 1) / 2;
+      std::vector<double> cm(lay.cm_len);
+      const double px = (double)d.map_len / nb;
+      for (int bx = 0; bx < nb; ++bx)
+        for (int by = 0; by <= bx; ++by) {
+          const int64_t k = (int64_t)bx * (bx + 1) / 2 + by;
+          const double self = bx == by ? px * d.n_copies : 0.0;
+          cm[k] = 1000.0 * (hmap[d.map_off + k] / (double)frames + self) / (d.n_copies * px * px);
+        }
+      ana.finish((int)s, lay, sd, cp, cm);
+    }
+    reset_observables();
+    sync_and_check();
+  }
+
   std::vector<unsigned long long> overlaps() {
     CK(cudaMemsetAsync(ovl.p, 0, sizeof(unsigned long long) * hsys.size(), stream));
     sort_now();
@@ -1342,6 +1451,65 @@ int ccpgpu_observe(ccpgpu_sim *h, int32_t with_sdist) {
     need(h, "null argument");
     h->e->observe(with_sdist != 0);
   });
+}
+
+int ccpgpu_analysis_frame(ccpgpu_sim *h) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->analysis_frame();
+  });
+}
+
+int ccpgpu_analysis_series(ccpgpu_sim *h, int32_t sys, float *out, size_t n, int32_t *frames) {
+  return guarded([&] {
+    need(h && frames, "null argument");
+    sys_of(h, sys);
+    const Engine &e = *h->e;
+    const int f = e.ana.series.empty() ? 0 : e.ana.frames(sys);
+    *frames = f;
+    if (!out) return;
+    need(n >= (size_t)ANA_SERIES * f, "buffer too small");
+    for (int k = 0; k < ANA_SERIES; ++k)
+      std::copy(e.ana.series[sys][k].begin(), e.ana.series[sys][k].end(), out + (size_t)k * f);
+  });
+}
+
+int ccpgpu_analysis_end_simulation(ccpgpu_sim *h) {
+  return guarded([&] {
+    need(h, "null argument");
+    h->e->analysis_end();
+  });
+}
+
+int ccpgpu_analysis_txt(ccpgpu_sim *h, int32_t sys, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    sys_of(h, sys);
+    const Engine &e = *h->e;
+    if (e.ana.last_txt.empty() || e.ana.last_txt[sys].empty())
+      throw Error(ST_STATE, "no finished analysis simulation");
+    rc = put_bytes(e.ana.last_txt[sys], buf, cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_analysis_fin_txt(ccpgpu_sim *h, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    rc = put_bytes(h->e->ana.final_txt(), buf, cap, len);
+  });
+  return g ? g : rc;
+}
+
+int ccpgpu_contact_map_bin(ccpgpu_sim *h, char *buf, size_t cap, size_t *len) {
+  int rc = CCPGPU_OK;
+  int g = guarded([&] {
+    need(h, "null argument");
+    rc = put_bytes(h->e->ana.contact_map_bin(), buf, cap, len);
+  });
+  return g ? g : rc;
 }
 
 int ccpgpu_reset_observables(ccpgpu_sim *h) {

@@ -1140,6 +1140,38 @@ __global__ void __launch_bounds__(OBS_WARPS * 32)
   }
 }
 
+// Per-frame nematic order parameter and nucleus chromatin fraction sums of
+// every system (chrana.cu:396-418): fx[2 s] += over beads i < n - 1 of the
+// system (3 cos^2 - 1) / 2, cos the angle between the bond i -> i + 1 and
+// r_i (over chain ends too, as ccp); fx[2 s + 1] += beads with z < nod. FP64.
+__global__ void __launch_bounds__(256)
+    k_frame_extra(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                  const float4 *__restrict__ pos, double *__restrict__ fx) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  const int i = t.begin + threadIdx.x;
+  const int end = s.bead_off + s.n;
+  double nop = 0.0, ncf = 0.0;
+  if (i < end) {
+    const float4 p = pos[i];
+    if (p.z < s.nod) ncf = 1.0;
+    if (i + 1 < end) {
+      const float4 q = pos[i + 1];
+      const double bx = (double)q.x - p.x, by = (double)q.y - p.y, bz = (double)q.z - p.z;
+      const double c = (bx * p.x + by * p.y + bz * p.z) /
+                       (sqrt(bx * bx + by * by + bz * bz) *
+                        sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z));
+      nop = 0.5 * (3.0 * c * c - 1.0);
+    }
+  }
+  nop = warp_sum_d(nop);
+  ncf = warp_sum_d(ncf);
+  if ((threadIdx.x & 31) == 0) {
+    if (nop != 0.0) atomicAdd(&fx[2 * t.sys], nop);
+    if (ncf != 0.0) atomicAdd(&fx[2 * t.sys + 1], ncf);
+  }
+}
+
 // Mean spatial distance by separation (the sd part of calc_sd_cp,
 // chrana.cu:13-45): ds[chain_ps_off + s] += sum_p |r_{p+s} - r_p| over a chunk
 // of p, FP32 distances accumulated in FP64.
