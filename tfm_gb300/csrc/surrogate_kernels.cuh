@@ -8,8 +8,9 @@
 //    input window of the tile's pixels plus a margin on both sides
 //    (out-of-image pixels arrive as zeros, which is the convolution's zero
 //    padding); each tap of the row reads it at its own row offset. The
-//    weights of all taps stay resident in shared memory. Accumulators live in TMEM,
-//    double-buffered so the epilogue of one tile overlaps the MMAs of the next.
+//    weights of all taps stay resident in shared memory. Accumulators live in
+//    TMEM, 256 / N of them, so the epilogue of one tile overlaps the MMAs of
+//    the next ones; the epilogue loads its global inputs before it waits.
 //    The epilogue fuses bias, ReLU, the residual add, the ReLU mask bits and
 //    the gradient masking of the backward pass. The same kernel computes the
 //    input gradient of a convolution with negated tap offsets and transposed
@@ -36,12 +37,16 @@ namespace sur {
 using bf16 = __nv_bfloat16;
 
 constexpr int MAX_TAPS = 9;
-// warp 0: TMA, warp 1: MMA + TMEM, warps 2-9: epilogue (two warps per TMEM
-// lane quarter, each taking half of the output channels)
-constexpr int CONV_THREADS = 320;
+// warp 0: TMA; warps 1-2: MMA issue, alternate tiles (warp 1 also owns
+// TMEM); warps 3-10: epilogue (two warps per TMEM lane quarter, each taking
+// half of the output channels). Two issuing warps keep the tensor core fed:
+// one thread issues a 128 x N x 16 MMA every ~90 cycles, the tensor core
+// runs a 128 x 64 x 16 MMA every 48.
+constexpr int MMA_WARPS = 2;
+constexpr int CONV_THREADS = 32 * (1 + MMA_WARPS + 8);
 constexpr int EPI_WARPS = 8;
 constexpr int MAX_STAGES = 8;
-constexpr uint32_t TMEM_COLS_CONV = 256;  // two accumulators of up to 128 columns
+constexpr uint32_t TMEM_COLS_CONV = 256;  // 256 / N accumulators of N columns
 
 // A-operand windows: the input pixels [w0 - WIN_RADIUS, w0 + 128 + WIN_RADIUS)
 // of one image row, so that every tap of that row (column offset |dw| <=
@@ -126,34 +131,47 @@ __device__ __forceinline__ void store_bf16x16(bf16 *dst, const float *v) {
   d[1] = b;
 }
 
-// Epilogue of one output pixel p for the thread's half of the N channels
-// (32 N / 64 columns from TMEM address taddr): all global loads of the row
-// are issued before the accumulator is read so their latencies overlap.
-// Returns this thread's partial output-layer dot (0 without wo).
+// Global inputs of one output pixel's epilogue, loaded before the
+// accumulator is ready so their latency overlaps the tile's MMAs.
 template <int N>
-__device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float *sbias, const float *swo,
-                                                   size_t p, int half, uint32_t taddr) {
+struct EpiLoads {
+  uint4 rb[N / 64][4];
+  float4 rf[N / 64][8];
+  uint32_t mi[N / 64];
+  float rdy;
+};
+
+template <int N>
+__device__ __forceinline__ void conv_epilogue_load(const ConvEpi &e, size_t p, int half, EpiLoads<N> &ld) {
   constexpr int G = N / 64;  // 32-column groups per thread
   const int c_begin = half * (N / 2);
-  uint4 rb[G][4];
-  float4 rf[G][8];
-  uint32_t mi[G];
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const size_t o = p * (size_t)N + c_begin + 32 * g;
     if (e.resid) {
       const uint4 *s = reinterpret_cast<const uint4 *>(e.resid + o);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) rb[g][i] = s[i];
+      for (int i = 0; i < 4; ++i) ld.rb[g][i] = s[i];
     }
     if (e.resid_f32) {
       const float4 *s = reinterpret_cast<const float4 *>(e.resid_f32 + o);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) rf[g][i] = s[i];
+      for (int i = 0; i < 8; ++i) ld.rf[g][i] = s[i];
     }
-    if (e.mask_in) mi[g] = e.mask_in[p * (N / 32) + (c_begin >> 5) + g];
+    if (e.mask_in) ld.mi[g] = e.mask_in[p * (N / 32) + (c_begin >> 5) + g];
   }
-  const float rdy = e.resid_dy ? e.resid_dy[p] : 0.0f;
+  ld.rdy = e.resid_dy ? e.resid_dy[p] : 0.0f;
+}
+
+// Epilogue of one output pixel p for the thread's half of the N channels
+// (32 N / 64 columns from TMEM address taddr), with its global inputs in ld.
+// Returns this thread's partial output-layer dot (0 without wo).
+template <int N>
+__device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float *sbias, const float *swo,
+                                                   size_t p, int half, uint32_t taddr, const EpiLoads<N> &ld) {
+  constexpr int G = N / 64;
+  const int c_begin = half * (N / 2);
+  const float rdy = ld.rdy;
   float dot = 0.0f;
 #pragma unroll
   for (int g = 0; g < G; ++g) {
@@ -177,7 +195,7 @@ __device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float
     if (e.resid) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const uint32_t w[4] = {rb[g][i].x, rb[g][i].y, rb[g][i].z, rb[g][i].w};
+        const uint32_t w[4] = {ld.rb[g][i].x, ld.rb[g][i].y, ld.rb[g][i].z, ld.rb[g][i].w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           v[8 * i + 2 * k] += bf_lo(w[k]);
@@ -188,10 +206,10 @@ __device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float
     if (e.resid_f32) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        v[4 * i] += rf[g][i].x;
-        v[4 * i + 1] += rf[g][i].y;
-        v[4 * i + 2] += rf[g][i].z;
-        v[4 * i + 3] += rf[g][i].w;
+        v[4 * i] += ld.rf[g][i].x;
+        v[4 * i + 1] += ld.rf[g][i].y;
+        v[4 * i + 2] += ld.rf[g][i].z;
+        v[4 * i + 3] += ld.rf[g][i].w;
       }
     }
     if (e.resid_dy) {
@@ -210,7 +228,7 @@ __device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float
     }
     if (e.mask_in) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = ((mi[g] >> i) & 1u) ? v[i] : 0.0f;
+      for (int i = 0; i < 32; ++i) v[i] = ((ld.mi[g] >> i) & 1u) ? v[i] : 0.0f;
     }
     if (e.out) {
       store_bf16x16(e.out + o, v);
@@ -237,9 +255,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
   const uint32_t w_base = base;
   const uint32_t a_base = w_base + (uint32_t)nwt * w_tile;
   const uint32_t bar0 = a_base + (uint32_t)S * WIN_BYTES;
-  // barriers: full[S], empty[S], tfull[2], tempty[2], weights, fin
+  // TMEM accumulators: ACC buffers of N columns within TMEM_COLS_CONV
+  constexpr int ACC = (int)TMEM_COLS_CONV / N;
+  // barriers: full[S], empty[S], tfull[ACC], tempty[ACC], weights, fin
   const uint32_t full0 = bar0, empty0 = bar0 + 8u * S, tfull0 = bar0 + 16u * S,
-                 tempty0 = tfull0 + 16u, wbar = tempty0 + 16u, fin = wbar + 8u;
+                 tempty0 = tfull0 + 8u * ACC, wbar = tempty0 + 8u * ACC, fin = wbar + 8u;
   uint8_t *tail = smem_raw + (bar0 + 256u - raw);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tail);
   volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
@@ -252,12 +272,12 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       tc::mbar_init(full0 + 8u * s, 1);
       tc::mbar_init(empty0 + 8u * s, 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < ACC; ++b) {
       tc::mbar_init(tfull0 + 8u * b, 1);
       tc::mbar_init(tempty0 + 8u * b, EPI_WARPS);
     }
     tc::mbar_init(wbar, 1);
-    tc::mbar_init(fin, 1);
+    tc::mbar_init(fin, MMA_WARPS);
     *abort = 0;
     tc::fence_barrier_init();
   }
@@ -310,21 +330,25 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
         tc::mbar_drain(full0 + 8u * s, ph);
       }
     }
-  } else if (warp == 1) {
+  } else if (warp <= MMA_WARPS) {
     if (lane == 0) {
-      // ---- MMA issuer
+      // ---- MMA issuer m takes the CTA's tiles local = m, m + MMA_WARPS, ...
+      const int m = warp - 1;
       constexpr uint32_t idesc = tc::idesc_bf16(128, N, false, false);
       // descriptor bits other than the start address (bits 0-13; shared
       // memory addresses are below 2^18)
       const uint64_t desc_hi = tc::sdesc(0u, 16u, 1024u);
-      int s = 0;
-      uint32_t ph = 0;
-      int local = 0;
+      constexpr uint32_t KB = (uint32_t)(R * CB);  // windows per tile
+      int local = m;
       if (tc::mbar_wait(wbar, 0, abort)) {
-        for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
-          const int buf = local & 1;
-          if (!tc::mbar_wait(tempty0 + 8u * buf, (((uint32_t)local >> 1) & 1u) ^ 1u, abort)) break;
+        for (int tile = blockIdx.x + m * gridDim.x; tile < sh.n_tiles;
+             tile += MMA_WARPS * gridDim.x, local += MMA_WARPS) {
+          const int buf = local % ACC;
+          if (!tc::mbar_wait(tempty0 + 8u * buf, (((uint32_t)(local / ACC)) & 1u) ^ 1u, abort)) break;
           tc::fence_after_sync();
+          // this tile's windows: global window indices local * KB ...
+          int s = (int)(((uint32_t)local * KB) % (uint32_t)S);
+          uint32_t ph = (((uint32_t)local * KB) / (uint32_t)S) & 1u;
           const uint32_t d = tmem + (uint32_t)(buf * N);
           uint32_t acc = 0;
           bool ok = true;
@@ -364,18 +388,20 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
   } else {
     // ---- epilogue: warp w reads TMEM lanes 32 (w mod 4) .. +31, half of the columns
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
+    const int half = (warp - 1 - MMA_WARPS) >> 2;
     const int row = q * 32 + lane;
     int local = 0;
     for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
-      const int buf = local & 1;
-      const uint32_t use = (uint32_t)local >> 1;
-      if (!tc::mbar_wait(tfull0 + 8u * buf, use & 1u, abort)) break;
-      tc::fence_after_sync();
+      const int buf = local % ACC;
+      const uint32_t use = (uint32_t)(local / ACC);
       const int wb = tile % wtiles, bh = tile / wtiles;
       const size_t p = (size_t)bh * sh.W + (size_t)wb * 128 + row;
+      EpiLoads<N> ld;
+      conv_epilogue_load<N>(epi, p, half, ld);  // before the accumulator is ready
+      if (!tc::mbar_wait(tfull0 + 8u * buf, use & 1u, abort)) break;
+      tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N);
-      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr);
+      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr, ld);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tempty0 + 8u * buf);
