@@ -105,10 +105,21 @@ int ccpgpu_system_info_get(const ccpgpu_sim *h, int32_t sys, ccpgpu_system_info 
 
 /* ---------------------------------------------------------------- simulation */
 
-/* chrsim::generate_initial_condition (chrsim.cu:470-522): LBS placement, type
- * sequence, confined random walk, then soft-repulsion relaxation on the GPU
- * until no non-bonded pair is closer than 0.838732. */
+/* chrsim::generate_initial_condition (chrsim.cu:470-522): LBS placement and
+ * type sequence on the host, then the confined random walk and the
+ * soft-repulsion relaxation on the GPU until no non-bonded pair is closer
+ * than 0.838732. */
 int ccpgpu_generate_initial_condition(ccpgpu_sim *h);
+
+/* chrsim::set_particle_positons + perform_random_walk (chrsim.cu:678-802):
+ * the confined random walk of every chain with the current types, without the
+ * relaxation. ccp's 30386-bead diploid model walks its 12 chromosomes in cones
+ * around shuffled icosahedral directions; other chains walk without a cone.
+ * Chain c of a system draws attempt k from Philox4x32-10 keyed by the
+ * system's seed with counter (k, c, 0x10057, 0x1C0DE). draws (NULL allowed,
+ * n >= total chains) receives each chain's number of attempts. Returns
+ * CCPGPU_ERR_STATE when a chain exceeds 256 attempts per bead + 2^17. */
+int ccpgpu_random_walk(ccpgpu_sim *h, uint32_t *draws, size_t n);
 
 /* chrsim::run_simulation (chrsim.cu:558-593): frames_per_file frames of
  * steps_per_frame Heun steps; after each frame i_f += 1, t += spf * dt and fn
@@ -151,7 +162,8 @@ int ccpgpu_autotune(ccpgpu_sim *h, int32_t reps, char *report, size_t cap, size_
 int ccpgpu_kernel_count(const ccpgpu_sim *h, uint64_t *count);
 
 /* Device error flags: [0] non-finite position, [1] bead outside its grid,
- * [2] counting-sort slot outside its system, [3] noise truncation exhausted.
+ * [2] counting-sort slot outside its system, [3] noise truncation exhausted,
+ * [4] random-walk draw budget exhausted.
  * clear != 0 resets them. Returns CCPGPU_ERR_STATE when [0] or [2] is set. */
 int ccpgpu_error_flags(ccpgpu_sim *h, int32_t *flags8, int32_t clear);
 

@@ -19,6 +19,7 @@
  *   contact map             chrana.cu:48-84     (calc_cm)
  *   d(s), P(s)              chrana.cu:13-45     (calc_sd_cp)
  *   Rg^2, radial density    chrana.cu:372-480   (calc_observables)
+ *   confined random walk    chrsim.cu:678-802   (perform_random_walk)
  * The noise generator is the published Philox4x32-10 (Salmon et al., SC'11)
  * with Box-Muller, keyed exactly like the engine (the reference seeds cuRAND
  * with time(nullptr), so its noise is not reproducible and is not pinned).
@@ -232,6 +233,103 @@ void orc_sdist(int L, const float *xyz, double *ds) {
     }
     ds[s] = acc;
   }
+}
+
+/* ------------------------------------------------------------ random walk */
+
+/* Inverse error function by Newton iteration on erf (erf'(x) =
+ * 2/sqrt(pi) exp(-x^2)), from the start 0.5 ln((1+y)/(1-y)) / 1.2; +-inf at
+ * |y| >= 1. */
+static double erfinv_newton(double y) {
+  if (y <= -1.0) return -INFINITY;
+  if (y >= 1.0) return INFINITY;
+  double x = 0.5 * log((1.0 + y) / (1.0 - y)) / 1.2;
+  for (int k = 0; k < 100; ++k) {
+    double e = erf(x) - y, d = 1.1283791670955126 * exp(-x * x);
+    if (d == 0.0) break;
+    double st = e / d;
+    if (st > 1.0) st = 1.0;
+    if (st < -1.0) st = -1.0;
+    x -= st;
+    if (fabs(st) < 1e-15 * (fabs(x) > 1.0 ? fabs(x) : 1.0)) break;
+  }
+  return x;
+}
+
+static double u24(uint32_t x) { return (double)((x >> 8) + 1u) / 16777216.0; }
+
+/* Confined random walk of one chain of n beads, in double
+ * (chrsim::perform_random_walk, chrsim.cu:719-802), on the engine's stream:
+ * attempt k draws the Philox block of counter (k, chain, 0x10057, 0x1C0DE)
+ * keyed by the system seed (two uniforms for the direction, one for the bond
+ * angle, one for the bond length; the first bead uses three). Sequential: an
+ * attempt is accepted when the position is finite, at least mis from the wall
+ * and (axis non-zero) inside the cone acos(r.a/|r||a|) <= mda; after more
+ * than 1024 consecutive rejections every rejection moves back to bead
+ * 1 + i*3/4 (then on to the next), the rejected candidate staying written.
+ * c_b: the density of cos(bond angle) is exp(c_b cos). Returns the attempts used, or
+ * -1 when max_draws ran out; *n_back (if not NULL) counts the moves back. */
+long long orc_random_walk(int n, double *xyz, uint32_t k0, uint32_t k1, uint32_t chain,
+                          const double *axis, double cos_mda, double R_n, double mis,
+                          double c_b, double l_0, double sig_b, long long max_draws,
+                          long long *n_back) {
+  if (n_back) *n_back = 0;
+  double la = sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+  long long draw = 0;
+  uint32_t o[4];
+  double old[3], d_r;
+  for (;;) {
+    if (draw >= max_draws) return -1;
+    uint32_t c[4] = {(uint32_t)draw++, chain, 0x10057u, 0x1C0DEu};
+    philox10(c, k0, k1, o);
+    double ct = 1.0 - 2.0 * u24(o[0]), st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    double ph = 2.0 * M_PI * u24(o[1]);
+    old[0] = st * cos(ph);
+    old[1] = st * sin(ph);
+    old[2] = ct;
+    d_r = (R_n - mis) * cbrt(u24(o[2]));
+    for (int a = 0; a < 3; ++a) xyz[a] = d_r * old[a];
+    if (la == 0.0) break;
+    /* acos(r.a / (|r| |a|)) > mda rejects: r.a < cos(mda) |r| |a| */
+    if (!(xyz[0] * axis[0] + xyz[1] * axis[1] + xyz[2] * axis[2] < cos_mda * d_r * la)) break;
+  }
+  const double one_m_e = 1.0 - exp(-2.0 * c_b);
+  int att = 0;
+  for (int i = 1; i < n; ++i) {
+    if (draw >= max_draws) return -1;
+    uint32_t c[4] = {(uint32_t)draw++, chain, 0x10057u, 0x1C0DEu};
+    philox10(c, k0, k1, o);
+    double ct = 1.0 - 2.0 * u24(o[0]), st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    double ph = 2.0 * M_PI * u24(o[1]);
+    double rd[3] = {st * cos(ph), st * sin(ph), ct};
+    double per[3] = {old[1] * rd[2] - old[2] * rd[1], old[2] * rd[0] - old[0] * rd[2],
+                     old[0] * rd[1] - old[1] * rd[0]};
+    double il = 1.0 / sqrt(per[0] * per[0] + per[1] * per[1] + per[2] * per[2]);
+    double cb = 1.0 + log1p(-one_m_e * u24(o[2])) * (1.0 / c_b);
+    if (cb > 1.0) cb = 1.0;
+    if (cb < -1.0) cb = -1.0;
+    double sb = sqrt(1.0 - cb * cb) * il;
+    double lb = l_0 + sig_b * erfinv_newton(2.0 * u24(o[3]) - 1.0);
+    double nd[3], *p = xyz + 3 * (size_t)i, *q = xyz + 3 * (size_t)(i - 1);
+    for (int a = 0; a < 3; ++a) {
+      nd[a] = cb * old[a] + sb * per[a];
+      p[a] = lb * nd[a] + q[a];
+    }
+    int ok = isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]);
+    double dr = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    if ((R_n - dr) < mis) ok = 0;
+    if (la != 0.0 && p[0] * axis[0] + p[1] * axis[1] + p[2] * axis[2] < cos_mda * dr * la) ok = 0;
+    if (ok) {
+      att = 0;
+      for (int a = 0; a < 3; ++a) old[a] = nd[a];
+    } else if ((att = att < (1 << 20) ? att + 1 : att) > 1024) {
+      i = 1 + i * 3 / 4;
+      if (n_back) ++*n_back;
+    } else {
+      --i;
+    }
+  }
+  return draw;
 }
 
 int orc_max_threads(void) {

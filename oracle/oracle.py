@@ -94,6 +94,8 @@ def lib():
         L.orc_overlaps.restype = C.c_longlong
         L.orc_observables.argtypes = [I, P, P, D, D, P]
         L.orc_sdist.argtypes = [I, P, P]
+        L.orc_random_walk.argtypes = [I, P, U32, U32, U32, P, D, D, D, D, D, D, C.c_longlong, P]
+        L.orc_random_walk.restype = C.c_longlong
         L.orc_max_threads.restype = I
         _lib = L
     return _lib
@@ -186,3 +188,49 @@ def sdist(xyz):
     ds = np.zeros(L // 2 + 1, np.float64)
     lib().orc_sdist(L, _p(xyz), _p(ds))
     return ds
+
+
+def host_uniforms(seed, stream_id, n):
+    """(0, 1] uniforms of the engine's host initial-condition stream: Philox
+    counter (ctr lo, ctr hi, 0x10000, 0x1C0DE) from ctr = stream_id << 40."""
+    out, ctr = [], stream_id << 40
+    key = [seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF]
+    while len(out) < n:
+        o = philox([ctr & 0xFFFFFFFF, ctr >> 32, 0x10000, 0x1C0DE], key)
+        out += [((int(v) >> 8) + 1) / 16777216.0 for v in o]
+        ctr += 1
+    return out[:n]
+
+
+def walk_axes(seed, diploid, n_chains):
+    """Cone axes and cos(half-angle) of set_particle_positons (chrsim.cu:678-716):
+    ccp's diploid model shuffles the 12 icosahedral directions (Fisher-Yates,
+    j = (i + 1)(1 - u)) and walks chain c around direction c % 12 within
+    pi/2 - atan(golden ratio); other chains have no cone."""
+    if not diploid:
+        return [(0.0, 0.0, 0.0)] * n_chains, math.cos(math.pi)
+    phi = (1.0 + math.sqrt(5.0)) / 2.0
+    d = [(0, 1, phi), (1, phi, 0), (phi, 0, 1), (0, 1, -phi), (1, -phi, 0), (-phi, 0, 1),
+         (0, -1, phi), (-1, phi, 0), (phi, 0, -1), (0, -1, -phi), (-1, -phi, 0), (-phi, 0, -1)]
+    u = host_uniforms(seed, 0x52, 11)
+    for k, i in enumerate(range(11, 0, -1)):
+        j = int((i + 1) * (1.0 - float(np.float32(u[k]))))
+        d[i], d[j] = d[j], d[i]
+    return [d[c % 12] for c in range(n_chains)], math.cos(math.pi / 2.0 - math.atan(phi))
+
+
+def random_walk(n, seed, chain, axis, cos_mda, R_n, kT=1.0, k_b=1.0, k_e=128.0, l_0=1.0,
+                mis=MIS, max_draws=None, with_backs=False):
+    """One chain's confined random walk (oracle/ccp_oracle.c orc_random_walk);
+    returns (positions (n, 3) float64, attempts used or -1[, moves back])."""
+    xyz = np.zeros((n, 3), np.float64)
+    ax = np.asarray(axis, np.float64)
+    iT = 1.0 / kT
+    c_b = 0.5 * iT * k_b
+    nb = np.zeros(1, np.int64)
+    budget = max_draws if max_draws is not None else min(256 * n + (1 << 17), 0xFFFFFF00)
+    used = lib().orc_random_walk(n, _p(xyz), seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF, chain,
+                                 _p(ax), cos_mda, R_n, mis, c_b, l_0,
+                                 math.sqrt(2.0 / (k_e * iT)), budget, _p(nb))
+    return (xyz, used, int(nb[0])) if with_backs else (xyz, used)
+

@@ -34,3 +34,29 @@ def force_errors(f_gpu, f_ref, absum):
     rel = (d[big] / n[big]).max() if big.any() else 0.0
     scaled = (d / np.maximum(absum, 1e-30)).max()
     return rel, scaled
+
+
+def at_cutoff(x, fl, lbs, ff, tol=1e-5):
+    """Beads with an attractive (A-A) pair or a lamina-binding site within tol
+    of its cutoff. The baseline force field's truncated Lennard-Jones force
+    jumps there, so FP32 and FP64 distances may fall on opposite sides of the
+    cutoff and the two forces differ by the jump; such beads are checked
+    against the jump's size instead."""
+    from scipy.spatial import cKDTree
+
+    x = np.asarray(x, np.float64)
+    hit = np.zeros(len(x), bool)
+    a = np.flatnonzero(fl & 1)
+    if len(a) > 1:
+        t = cKDTree(x[a])
+        for i, j in t.query_pairs(ff["rc_att"] + tol, output_type="ndarray"):
+            if abs(np.linalg.norm(x[a[i]] - x[a[j]]) - ff["rc_att"]) < tol:
+                hit[a[i]] = hit[a[j]] = True
+    lad = np.flatnonzero(fl & 2)
+    if len(lad) and len(lbs):
+        t = cKDTree(np.asarray(lbs, np.float64).reshape(-1, 3))
+        for k, near in enumerate(t.query_ball_point(x[lad], ff["lco"] + tol)):
+            for l in near:
+                if abs(np.linalg.norm(x[lad[k]] - t.data[l]) - ff["lco"]) < tol:
+                    hit[lad[k]] = True
+    return hit

@@ -12,7 +12,7 @@ has already run every other test; it also passes alone in a fresh process.
 import numpy as np
 import pytest
 
-from helpers import baseline_params, ccp_params
+from helpers import at_cutoff, baseline_params, ccp_params
 
 pytestmark = pytest.mark.gpu
 
@@ -29,13 +29,15 @@ def _reference(orc, text, seed, heads, ff, csl, preset):
     fl = orc.flags_from_types(pt, heads, preset)
     geo = orc.geo_vec(si.nucleus_radius, csl=csl)
     f64, sa = orc.forces(x, fl, np.zeros((0, 3), np.float32), ff, geo, with_abs=True, cells=True)
-    return x, pt, si.nucleus_radius, sim.forces(), f64, sa
+    edge = at_cutoff(x, fl, np.zeros((0, 3)), ff)
+    return x, pt, si.nucleus_radius, sim.forces(), f64, sa, edge
 
 
-def _bound(f, f_ref, sa):
+def _bound(f, f_ref, sa, skip=None):
     d = np.linalg.norm(np.asarray(f, np.float64) - np.asarray(f_ref, np.float64), axis=1)
     scale = np.maximum(np.maximum(np.linalg.norm(f_ref, axis=1), 0.1 * sa), 1.0)
-    return (d / scale).max()
+    e = d / scale
+    return (e[~skip] if skip is not None else e).max()
 
 
 def test_noalloc_forces_match_compute_forces(engine_lib, orc):
@@ -52,7 +54,7 @@ def test_noalloc_forces_match_compute_forces(engine_lib, orc):
     dev = torch.device("cuda:0")
     stream = torch.cuda.current_stream(dev)
     # two systems, then the first again: each call must not see the previous one
-    for preset, n, nch, (x, pt, R, f_alloc, f64, sa) in (cases[0], cases[1], cases[0]):
+    for preset, n, nch, (x, pt, R, f_alloc, f64, sa, edge) in (cases[0], cases[1], cases[0]):
         d_x = torch.tensor(x, device=dev)
         d_t = torch.tensor(pt, device=dev)
         d_f = torch.full((n, 3), float("nan"), dtype=torch.float32, device=dev)
@@ -63,7 +65,10 @@ def test_noalloc_forces_match_compute_forces(engine_lib, orc):
         f = d_f.cpu().numpy()
         assert np.isfinite(f).all()
         assert _bound(f, f_alloc, sa) <= FORCE_RTOL
-        assert _bound(f, f64, sa) <= FORCE_RTOL
+        # beads within FP32 rounding of a jump of the truncated potential are
+        # held to the jump's size (see helpers.at_cutoff)
+        assert _bound(f, f64, sa, skip=edge) <= FORCE_RTOL
+        assert _bound(f, f64, sa) <= 1e-2
 
     # sizes beyond the scratch are refused, not truncated
     big = ccpgpu.NOALLOC_MAX_BEADS + 1

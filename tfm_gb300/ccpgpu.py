@@ -34,7 +34,7 @@ SYMBOLS = (
     "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
     "ccpgpu_forces_noalloc", "ccpgpu_autotune", "ccpgpu_analysis_frame", "ccpgpu_analysis_series",
     "ccpgpu_analysis_end_simulation", "ccpgpu_analysis_txt", "ccpgpu_analysis_fin_txt",
-    "ccpgpu_contact_map_bin",
+    "ccpgpu_contact_map_bin", "ccpgpu_random_walk",
 )
 
 NOALLOC_MAX_BEADS = 32768
@@ -94,6 +94,7 @@ def load(path=LIB_PATH):
         "ccpgpu_info_get": [P, C.POINTER(Info)],
         "ccpgpu_system_info_get": [P, I32, C.POINTER(SystemInfo)],
         "ccpgpu_generate_initial_condition": [P],
+        "ccpgpu_random_walk": [P, P, SZ],
         "ccpgpu_run_simulation": [P, FRAME_FN, P],
         "ccpgpu_run_steps": [P, U64, U32],
         "ccpgpu_error_flags": [P, P, I32],
@@ -216,6 +217,13 @@ class _Handle:
 
     def generate_initial_condition(self):
         _check(_lib.ccpgpu_generate_initial_condition(self._h))
+
+    def random_walk(self):
+        """Confined random walk of every chain (no relaxation); returns each
+        chain's number of attempts."""
+        d = np.zeros(self.info().n_chains, np.uint32)
+        _check(_lib.ccpgpu_random_walk(self._h, _ptr(d), d.size))
+        return d
 
     def run_steps(self, n, observe_every=0):
         _check(_lib.ccpgpu_run_steps(self._h, int(n), int(observe_every)))

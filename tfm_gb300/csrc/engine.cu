@@ -930,16 +930,90 @@ struct Engine {
       else
         make_types_markov(d.n, par.mean_block, par.lad_fraction, rng, pt);
       std::copy(pt.begin(), pt.end(), hpt.begin() + d.bead_off);
-      std::vector<int> heads;
-      for (int c = 0; c < d.n_chains; ++c) heads.push_back(chain_first[d.chain_off + c] - d.bead_off);
-      bool diploid = par.preset == PRESET_CCP && (uint32_t)d.n == CCP_N_DEF && d.n_chains == 12;
-      std::vector<float> x;
-      random_walk(geo[s], ff, diploid, heads, d.n, rng, x);
-      std::copy(x.begin(), x.end(), hxyz.begin() + 3 * (size_t)d.bead_off);
     }
     upload_lbs();
-    upload_positions();
+    random_walk(nullptr);
     relax();
+    download_positions();
+  }
+
+  // Confined random walk of every chain (chrsim::set_particle_positons and
+  // perform_random_walk, chrsim.cu:678-802) on the GPU, one warp per chain.
+  // ccp's diploid model walks its 12 chromosomes in cones around the 12
+  // icosahedral directions, shuffled per system on the host; every other
+  // chain walks without a cone. Positions end up in pos (and hxyz); draws, if
+  // given, receives each chain's number of attempts.
+  void random_walk(uint32_t *draws) {
+    std::fill(hxyz.begin(), hxyz.end(), 0.0f);
+    upload_positions();  // flags; the walk overwrites every position
+    std::vector<WalkChain> wc((size_t)nch);
+    for (size_t s = 0; s < hsys.size(); ++s) {
+      const SysDesc &d = hsys[s];
+      bool diploid = par.preset == PRESET_CCP && (uint32_t)d.n == CCP_N_DEF && d.n_chains == 12;
+      const double phi = (1.0 + std::sqrt(5.0)) / 2.0;
+      double dir[12][3] = {{0, 1, phi},  {1, phi, 0},  {phi, 0, 1},   {0, 1, -phi},
+                           {1, -phi, 0}, {-phi, 0, 1}, {0, -1, phi},  {-1, phi, 0},
+                           {phi, 0, -1}, {0, -1, -phi}, {-1, -phi, 0}, {-phi, 0, -1}};
+      if (diploid) {  // chrsim.cu:694-703
+        HostRng rng(specs[s].seed, 0x52u);
+        for (int i = 11; i > 0; --i) {
+          float ran = rng.uniform();
+          int j = (int)((i + 1) * (1.0 - ran));
+          for (int a = 0; a < 3; ++a) std::swap(dir[i][a], dir[j][a]);
+        }
+      }
+      const double mda = diploid ? M_PI / 2.0 - std::atan(phi) : M_PI;
+      for (int c = 0; c < d.n_chains; ++c) {
+        int g = d.chain_off + c;
+        WalkChain &w = wc[g];
+        w.first = chain_first[g];
+        w.end = (c + 1 < d.n_chains) ? chain_first[g + 1] : d.bead_off + d.n;
+        w.k0 = d.seed_lo;
+        w.k1 = d.seed_hi;
+        w.chain = (uint32_t)c;
+        uint64_t budget = 256ull * (uint64_t)(w.end - w.first) + (1ull << 17);
+        w.max_draws = (uint32_t)std::min<uint64_t>(budget, 0xFFFFFF00ull);
+        w.ax = diploid ? dir[c % 12][0] : 0.0;
+        w.ay = diploid ? dir[c % 12][1] : 0.0;
+        w.az = diploid ? dir[c % 12][2] : 0.0;
+        w.cos_mda = std::cos(mda);
+        w.R_n = d.R_n;
+      }
+    }
+    WalkParams wp;
+    const double iT = 1.0 / ff.kT;
+    const double kb = (ff.k_b > 0.0f) ? ff.k_b : 1.0;
+    const double c_b = 0.5 * iT * kb;
+    wp.inv_cb = 1.0 / c_b;
+    wp.one_m_e = 1.0 - std::exp(-2.0 * c_b);
+    wp.l_0 = ff.l_0;
+    wp.sig_b = std::sqrt(2.0 / (ff.k_e * iT));
+    wp.mis = ff.mis;
+    DevBuf<WalkChain> d_wc;
+    DevBuf<uint32_t> d_draws;
+    DevBuf<double> wxyz;
+    d_wc.alloc(std::max<size_t>(wc.size(), 1));
+    d_draws.alloc(std::max<size_t>(wc.size(), 1));
+    wxyz.alloc((size_t)3 * std::max(nb, 1));
+    CK(cudaMemcpyAsync(d_wc.p, wc.data(), sizeof(WalkChain) * wc.size(), cudaMemcpyHostToDevice,
+                       stream));
+    CK(cudaMemsetAsync(d_err.p + ERR_WALK, 0, sizeof(int), stream));
+    k_random_walk<<<(unsigned)((nch + WALK_WARPS - 1) / WALK_WARPS), 32 * WALK_WARPS, 0, stream>>>(
+        d_wc.p, nch, wp, pos.p, wxyz.p, d_draws.p, d_err.p);
+    CK(cudaGetLastError());
+    kcount += 1;
+    recount();
+    std::vector<uint32_t> used(wc.size());
+    CK(cudaMemcpyAsync(used.data(), d_draws.p, sizeof(uint32_t) * used.size(),
+                       cudaMemcpyDeviceToHost, stream));
+    int e[ERR_COUNT];
+    CK(cudaMemcpyAsync(e, d_err.p, sizeof(e), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (e[ERR_WALK]) {
+      positions_valid = false;
+      throw Error(ST_STATE, "confined random walk used up its draw budget");
+    }
+    if (draws) std::copy(used.begin(), used.end(), draws);
     download_positions();
   }
 
@@ -1180,6 +1254,14 @@ int ccpgpu_generate_initial_condition(ccpgpu_sim *h) {
   return guarded([&] {
     need(h, "null argument");
     h->e->generate_initial_condition();
+  });
+}
+
+int ccpgpu_random_walk(ccpgpu_sim *h, uint32_t *draws, size_t n) {
+  return guarded([&] {
+    need(h, "null argument");
+    need(!draws || n >= (size_t)h->e->nch, "buffer too small");
+    h->e->random_walk(draws);
   });
 }
 

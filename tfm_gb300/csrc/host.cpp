@@ -268,29 +268,6 @@ inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
 inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float len(V3 a) { return std::sqrt(dot(a, a)); }
-inline V3 cross(V3 a, V3 b) {
-  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-
-// Inverse error function by Newton iteration on erf (from the definition
-// erf'(x) = 2/sqrt(pi) exp(-x^2)); returns +-inf at |y| >= 1.
-double erfinv_newton(double y) {
-  if (y <= -1.0) return -std::numeric_limits<double>::infinity();
-  if (y >= 1.0) return std::numeric_limits<double>::infinity();
-  // start from the inverse of the logistic-like bound erf(x) ~ tanh(1.2 x)
-  double x = 0.5 * std::log((1.0 + y) / (1.0 - y)) / 1.2;
-  for (int k = 0; k < 60; ++k) {
-    double e = std::erf(x) - y;
-    double d = 1.1283791670955126 * std::exp(-x * x);
-    if (d == 0.0) break;
-    double step = e / d;
-    if (step > 1.0) step = 1.0;
-    if (step < -1.0) step = -1.0;
-    x -= step;
-    if (std::fabs(step) < 1e-15 * std::max(1.0, std::fabs(x))) break;
-  }
-  return x;
-}
 
 V3 random_direction(HostRng &rng) {
   float ran = rng.uniform();
@@ -387,88 +364,6 @@ void make_types_markov(int N, float mean_block, float lad_fraction, HostRng &rng
     int32_t v = cur;
     if (rng.uniform() <= lad_fraction) v |= 2;
     pt[i] = v;
-  }
-}
-
-// Confined random walk of one chain (chrsim.cu:719-802).
-static void walk_chain(const Geometry &g, const ForceField &ff, int i_s, int i_e, V3 dir,
-                       float mda, HostRng &rng, std::vector<float> &xyz) {
-  auto R = [&](int i) { return V3{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]}; };
-  auto W = [&](int i, V3 v) {
-    xyz[3 * i] = v.x;
-    xyz[3 * i + 1] = v.y;
-    xyz[3 * i + 2] = v.z;
-  };
-  float len_d = len(dir);
-  float iT = 1.0f / ff.kT;
-  float kb = (ff.k_b > 0.0f) ? ff.k_b : 1.0f;
-  float c_b = 0.5f * iT * kb;
-  V3 old_dir;
-  float d_r;
-  do {
-    V3 rd = random_direction(rng);
-    float ran = rng.uniform();
-    d_r = (g.R_n - CCP_MIS) * std::pow(ran, 1.0 / 3);
-    W(i_s, d_r * rd);
-    old_dir = rd;
-  } while (std::acos(dot(R(i_s), dir) / (d_r * len_d)) > mda);
-  unsigned att = 0;
-  for (int i = i_s + 1; i < i_e; ++i) {
-    V3 rd = random_direction(rng);
-    V3 per = cross(old_dir, rd);
-    per = (1.0f / len(per)) * per;
-    float ran = rng.uniform();
-    float angle_b = std::acos(1.0 + std::log(1.0 - (1.0 - std::exp(-2.0 * c_b)) * ran) / c_b);
-    V3 nd = (float)std::cos(angle_b) * old_dir + (float)std::sin(angle_b) * per;
-    ran = rng.uniform();
-    float len_b = ff.l_0 + std::sqrt(2.0 / (ff.k_e * iT)) * erfinv_newton(2.0 * ran - 1.0);
-    V3 p = len_b * nd + R(i - 1);
-    W(i, p);
-    bool ok = std::isfinite(p.x) && std::isfinite(p.y) && std::isfinite(p.z);
-    float dr = len(p);
-    if ((g.R_n - dr) < CCP_MIS) ok = false;
-    if (std::acos(dot(p, dir) / (dr * len_d)) > mda) ok = false;
-    if (ok) {
-      att = 0;
-      old_dir = nd;
-    } else {
-      ++att;
-      if (att > 1024)
-        i = i_s + 1 + (i - i_s) * 3 / 4;
-      else
-        --i;
-    }
-  }
-}
-
-// chrsim::set_particle_positons (chrsim.cu:678-716): ccp's diploid model walks
-// each of its 12 chromosomes in a cone around a shuffled icosahedral
-// direction; otherwise every chain is an unconstrained confined walk.
-void random_walk(const Geometry &g, const ForceField &ff, bool ccp_diploid,
-                 const std::vector<int> &chain_first, int N, HostRng &rng,
-                 std::vector<float> &xyz) {
-  xyz.assign((size_t)3 * N, 0.0f);
-  int nc = (int)chain_first.size();
-  if (ccp_diploid) {
-    float phi = (1.0 + std::sqrt(5.0)) / 2.0;
-    float mda = M_PI / 2.0 - std::atan(phi);
-    V3 dir[12] = {{0, 1, phi},  {1, phi, 0},  {phi, 0, 1},  {0, 1, -phi},
-                  {1, -phi, 0}, {-phi, 0, 1}, {0, -1, phi}, {-1, phi, 0},
-                  {phi, 0, -1}, {0, -1, -phi}, {-1, -phi, 0}, {-phi, 0, -1}};
-    for (int i = 11; i > 0; --i) {
-      float ran = rng.uniform();
-      int j = (int)((i + 1) * (1.0 - ran));
-      std::swap(dir[i], dir[j]);
-    }
-    for (int c = 0; c < nc; ++c) {
-      int e = (c + 1 < nc) ? chain_first[c + 1] : N;
-      walk_chain(g, ff, chain_first[c], e, dir[c % 12], mda, rng, xyz);
-    }
-  } else {
-    for (int c = 0; c < nc; ++c) {
-      int e = (c + 1 < nc) ? chain_first[c + 1] : N;
-      walk_chain(g, ff, chain_first[c], e, V3{0, 0, 0}, (float)M_PI, rng, xyz);
-    }
   }
 }
 

@@ -119,16 +119,14 @@ struct HostRng {
   float uniform();  // (0, 1]
 };
 
-// Initial-condition pieces of one system (chrsim.cu:596-802).
+// Host initial-condition pieces of one system (chrsim.cu:596-675); the
+// confined random walk (chrsim.cu:678-802) runs on the GPU.
 void place_lbs(const Geometry &g, float lbs_depth, float lco, int n_l, HostRng &rng,
                std::vector<float> &xyz);
 void make_types_ccp(uint32_t N, const std::string &seq_file, HostRng &rng,
                     std::vector<int32_t> &pt);
 void make_types_markov(int N, float mean_block, float lad_fraction, HostRng &rng,
                        std::vector<int32_t> &pt);
-void random_walk(const Geometry &g, const ForceField &ff, bool ccp_diploid,
-                 const std::vector<int> &chain_first, int N, HostRng &rng,
-                 std::vector<float> &xyz);
 
 // ccp file formats (chrdat.cu:107-284, chrsim.cu:525-555, chrana.cu:363-369).
 std::string format_frame_txt(uint32_t i_f, float t, const std::vector<int32_t> &pt,

@@ -28,6 +28,7 @@ enum : int {
   ERR_ESCAPE = 1,    // bead outside its cell grid (clamped to the border)
   ERR_SLOT = 2,      // scatter slot outside the system range (inconsistent counts)
   ERR_NOISE = 3,     // truncated normal needed more than NOISE_MAX_ATTEMPTS draws
+  ERR_WALK = 4,      // a confined random walk used up its draw budget
   ERR_COUNT = 8,
 };
 
@@ -1197,6 +1198,192 @@ __global__ void __launch_bounds__(256)
 
 // Sets the device step counter (the first scan of the next step bumps it).
 __global__ void k_set_step(unsigned long long *step, unsigned long long v) { *step = v; }
+
+// ------------------------------------------------ initial condition: random walk
+
+// One chain of the confined random walk (chrsim::perform_random_walk,
+// chrsim.cu:719-802).
+struct WalkChain {
+  int32_t first, end;    // beads [first, end) of pos
+  uint32_t k0, k1;       // Philox key: the system's seed
+  uint32_t chain;        // chain index within its system (the stream)
+  uint32_t max_draws;    // draw budget of the chain
+  double ax, ay, az;     // cone axis; zero: no cone
+  double cos_mda;        // cosine of the cone half-angle
+  double R_n;            // nucleus radius
+};
+
+// Constants of the walk shared by every chain.
+struct WalkParams {
+  double inv_cb;   // 1 / c_b, c_b = 0.5 k_b / kT: cos(bond angle) has density exp(c_b cos)
+  double one_m_e;  // 1 - exp(-2 c_b)
+  double l_0;      // rest bond length
+  double sig_b;    // sqrt(2 kT / k_e): bond-length spread
+  double mis;      // smallest allowed distance to the wall
+};
+
+// Draw d of a chain: one Philox block per attempt (two uniforms for the random
+// direction, one for the bond angle, one for the bond length).
+__device__ __forceinline__ U32x4 walk_bits(const WalkChain &w, uint32_t d) {
+  U32x4 c{d, w.chain, (STREAM_INIT << 16) | 0x57u, 0x1C0DEu};
+  return philox4x32_10(c, w.k0, w.k1);
+}
+
+__device__ __forceinline__ double walk_u(uint32_t x) {
+  return (double)((x >> 8) + 1u) * (1.0 / 16777216.0);  // (0, 1], 24 bits
+}
+
+// Uniform direction on the sphere from two (0, 1] uniforms:
+// cos(theta) = 1 - 2 u, phi = 2 pi v.
+__device__ __forceinline__ double3 walk_direction(uint32_t a, uint32_t b) {
+  double ct = 1.0 - 2.0 * walk_u(a);
+  double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  double sp, cp;
+  sincospi(2.0 * walk_u(b), &sp, &cp);
+  return make_double3(st * cp, st * sp, ct);
+}
+
+// Cone test of the reference, acos(r.a / (|r| |a|)) > mda rejects, written
+// without the arc cosine and the division: r.a < cos(mda) |r| |a| rejects (a
+// NaN passes, as in the reference's comparison); a zero axis has no cone.
+__device__ __forceinline__ bool walk_in_cone(const WalkChain &w, double la, double3 p, double dr) {
+  if (la == 0.0) return true;
+  return !((p.x * w.ax + p.y * w.ay + p.z * w.az) < w.cos_mda * dr * la);
+}
+
+// One warp per chain, in FP64 (the walk is latency-bound; FP64 makes it
+// reproducible to rounding by a CPU restatement, decision for decision). The
+// walk is the reference's sequential rejection walk: attempts for a bead
+// continue until one is accepted (finite, at least mis from the wall, inside
+// the cone); after more than 1024 consecutive rejections every further
+// rejection moves to bead first + 2 + (i - first) * 3 / 4, continuing from the
+// position stored there (the last rejected candidate of a bead stays stored,
+// as in the reference). Lanes evaluate consecutive attempts of the same bead
+// at once -- attempt k of the chain always uses draw k -- and the lowest
+// accepted lane is the attempt the sequential walk accepts; a chunk never
+// extends past the attempt that triggers a move back. So the walk equals the
+// sequential one. Chunks start at one attempt and double after each chunk
+// that is rejected whole (up to 32), so a walk that is mostly accepted keeps
+// one lane busy. wxyz holds the FP64 positions the walk continues from; pos
+// receives them in FP32. A chain that exceeds its draw budget sets ERR_WALK.
+constexpr int WALK_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * WALK_WARPS)
+k_random_walk(const WalkChain *__restrict__ chains, int n_chains, WalkParams wp,
+              float4 *__restrict__ pos, double *__restrict__ wxyz,
+              uint32_t *__restrict__ draws_used, int *__restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * WALK_WARPS + (threadIdx.x >> 5);
+  if (c >= n_chains) return;
+  const WalkChain w = chains[c];
+  const double la = sqrt(w.ax * w.ax + w.ay * w.ay + w.az * w.az);
+  const double r_in = w.R_n - wp.mis;
+  const unsigned FULL = 0xFFFFFFFFu;
+  uint32_t draw = 0;
+  int chunk = 1;
+  double3 old, prev;
+  // first bead: radial distance (R_n - mis) u^(1/3) along a random direction
+  for (;;) {
+    if (draw + (uint32_t)chunk > w.max_draws) {
+      if (lane == 0) {
+        set_err(err, ERR_WALK);
+        draws_used[c] = draw;
+      }
+      return;
+    }
+    double3 d = make_double3(0.0, 0.0, 0.0), p = d;
+    bool ok = false;
+    if (lane < chunk) {
+      U32x4 r = walk_bits(w, draw + lane);
+      d = walk_direction(r.x, r.y);
+      double dr = r_in * cbrt(walk_u(r.z));
+      p = make_double3(dr * d.x, dr * d.y, dr * d.z);
+      ok = walk_in_cone(w, la, p, dr);
+    }
+    unsigned acc = __ballot_sync(FULL, ok);
+    if (acc) {
+      int j = __ffs(acc) - 1;
+      old = make_double3(__shfl_sync(FULL, d.x, j), __shfl_sync(FULL, d.y, j),
+                         __shfl_sync(FULL, d.z, j));
+      prev = make_double3(__shfl_sync(FULL, p.x, j), __shfl_sync(FULL, p.y, j),
+                          __shfl_sync(FULL, p.z, j));
+      draw += (uint32_t)j + 1u;
+      if (lane == 0) {
+        float4 v = pos[w.first];
+        pos[w.first] = make_float4((float)prev.x, (float)prev.y, (float)prev.z, v.w);
+        double *q = wxyz + 3 * (size_t)w.first;
+        q[0] = prev.x;
+        q[1] = prev.y;
+        q[2] = prev.z;
+      }
+      break;
+    }
+    draw += (uint32_t)chunk;
+    chunk = min(2 * chunk, 32);
+  }
+  int att = 0;
+  int i = w.first + 1;
+  chunk = 1;
+  while (i < w.end) {
+    const int m = (att >= 1024) ? 1 : min(chunk, 1025 - att);
+    if (draw + (uint32_t)m > w.max_draws) {
+      if (lane == 0) set_err(err, ERR_WALK);
+      break;
+    }
+    double3 p = prev, nd = old;
+    bool ok = false;
+    if (lane < m) {
+      U32x4 r = walk_bits(w, draw + lane);
+      double3 rd = walk_direction(r.x, r.y);
+      double3 per = make_double3(old.y * rd.z - old.z * rd.y, old.z * rd.x - old.x * rd.z,
+                                 old.x * rd.y - old.y * rd.x);
+      double il = rsqrt(per.x * per.x + per.y * per.y + per.z * per.z);
+      // cos of the bond angle by inversion of its density exp(c_b cos) on [-1, 1]
+      double cb = 1.0 + log1p(-wp.one_m_e * walk_u(r.z)) * wp.inv_cb;
+      if (cb > 1.0) cb = 1.0;  // comparisons keep a NaN (rejected, like acos(NaN))
+      if (cb < -1.0) cb = -1.0;
+      double sb = sqrt(1.0 - cb * cb) * il;
+      nd = make_double3(cb * old.x + sb * per.x, cb * old.y + sb * per.y, cb * old.z + sb * per.z);
+      double lb = wp.l_0 + wp.sig_b * erfinv(2.0 * walk_u(r.w) - 1.0);
+      p = make_double3(lb * nd.x + prev.x, lb * nd.y + prev.y, lb * nd.z + prev.z);
+      double dr = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+      ok = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && !((w.R_n - dr) < wp.mis) &&
+           walk_in_cone(w, la, p, dr);
+    }
+    unsigned acc = __ballot_sync(FULL, ok);
+    // the accepted candidate, or the last rejected one, stays stored at bead i
+    const int j = acc ? __ffs(acc) - 1 : m - 1;
+    if (lane == j) {
+      float4 v = pos[i];
+      pos[i] = make_float4((float)p.x, (float)p.y, (float)p.z, v.w);
+      double *q = wxyz + 3 * (size_t)i;
+      q[0] = p.x;
+      q[1] = p.y;
+      q[2] = p.z;
+    }
+    if (acc) {
+      old = make_double3(__shfl_sync(FULL, nd.x, j), __shfl_sync(FULL, nd.y, j),
+                         __shfl_sync(FULL, nd.z, j));
+      prev = make_double3(__shfl_sync(FULL, p.x, j), __shfl_sync(FULL, p.y, j),
+                          __shfl_sync(FULL, p.z, j));
+      draw += (uint32_t)j + 1u;
+      att = 0;
+      chunk = 1;
+      ++i;
+    } else {
+      draw += (uint32_t)m;
+      att = min(att + m, 1 << 20);  // only att > 1024 matters
+      chunk = min(2 * chunk, 32);
+      if (att > 1024) {
+        i = w.first + 2 + (i - w.first) * 3 / 4;
+        __syncwarp();
+        const double *q = wxyz + 3 * (size_t)(i - 1);
+        prev = make_double3(q[0], q[1], q[2]);
+      }
+    }
+  }
+  if (lane == 0) draws_used[c] = draw;
+}
 
 // Positions as packed xyz triples (the .trr / checkpoint layout).
 __global__ void k_pack_xyz(const float4 *__restrict__ pos, float *__restrict__ xyz, int n) {
