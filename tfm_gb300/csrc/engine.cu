@@ -99,11 +99,14 @@ struct Engine {
   DevBuf<unsigned long long> ovl, d_step;
   DevBuf<int> d_err;
   DevBuf<float> xyz_stage;
+  DevBuf<float> fstage[2];  // packed frames of run_simulation, alternating
   float *pinned[2] = {nullptr, nullptr};
   float4 *pin_up = nullptr;  // pinned staging of position uploads
   bool lbs_uploaded = false;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t cstream = nullptr;  // device-to-host frame copies
+  cudaEvent_t ev[2] = {nullptr, nullptr};       // frame copy done (cstream)
+  cudaEvent_t ev_pack[2] = {nullptr, nullptr};  // frame packed (stream)
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
   std::map<std::tuple<int, int, int>, uint64_t> graph_kernels;  // kernel nodes per graph
   uint64_t kcount = 0;  // engine kernels launched (graph nodes included)
@@ -114,7 +117,9 @@ struct Engine {
       if (pinned[k]) cudaFreeHost(pinned[k]);
       if (k == 0 && pin_up) cudaFreeHost(pin_up);
       if (ev[k]) cudaEventDestroy(ev[k]);
+      if (ev_pack[k]) cudaEventDestroy(ev_pack[k]);
     }
+    if (cstream) cudaStreamDestroy(cstream);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -215,7 +220,11 @@ struct Engine {
     hflags.assign(nb, 0);
 
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ev_pack[k], cudaEventDisableTiming));
+    }
     d_sys.alloc(ns);
     d_tiles.alloc(htiles.size());
     d_ctiles.alloc(hctiles.size());
@@ -245,7 +254,10 @@ struct Engine {
     d_step.alloc(1);
     d_err.alloc(ERR_COUNT);
     xyz_stage.alloc((size_t)3 * nb);
-    for (int k = 0; k < 2; ++k) CK(cudaMallocHost(&pinned[k], sizeof(float) * 3 * std::max(nb, 1)));
+    for (int k = 0; k < 2; ++k) {
+      fstage[k].alloc((size_t)3 * nb);
+      CK(cudaMallocHost(&pinned[k], sizeof(float) * 3 * std::max(nb, 1)));
+    }
     CK(cudaMallocHost(&pin_up, sizeof(float4) * (nb + 1)));
 
     CK(cudaMemcpyAsync(d_sys.p, hsys.data(), sizeof(SysDesc) * ns, cudaMemcpyHostToDevice, stream));
@@ -1034,37 +1046,47 @@ struct Engine {
   }
 
   // -------------------------------------------------------------- frames
-  // chrsim::run_simulation: fpf frames of spf steps; frame k's positions are
-  // copied while frame k+1 runs.
+  // chrsim::run_simulation (chrsim.cu:558-593): fpf frames of spf steps. The
+  // steps of frame k+1 are enqueued before the host waits for frame k, so the
+  // frame callback (the trajectory write) runs while the GPU computes the next
+  // frame. Frame k is packed into fstage[k & 1] on the compute stream and
+  // copied to pinned[k & 1] on the copy stream, so the copy does not hold up
+  // the next frame's steps either; packing frame k + 2 into the same staging
+  // buffer waits for that copy.
   void run_simulation(ccpgpu_frame_fn fn, void *user) {
     if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
     const SysDesc &d0 = hsys[0];
     int pending = -1;
     uint32_t pend_if = 0;
     float pend_t = 0;
+    auto deliver = [&](int k) {
+      CK(cudaEventSynchronize(ev[k]));
+      if (fn && fn(user, pend_if, pend_t, pinned[k] + 3 * (size_t)d0.bead_off, d0.n)) {
+        CK(cudaStreamSynchronize(cstream));
+        CK(cudaStreamSynchronize(stream));
+        throw Error(ST_IO, "frame callback failed");
+      }
+    };
     for (uint32_t ffi = 0; ffi < par.fpf; ++ffi) {
       run_steps(par.spf, MODE_DST, 0);
       int b = ffi & 1;
-      k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(pos.p, xyz_stage.p, nb);
+      if (ffi >= 2) CK(cudaStreamWaitEvent(stream, ev[b], 0));
+      k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(pos.p, fstage[b].p, nb);
       CK(cudaGetLastError());
-      CK(cudaMemcpyAsync(pinned[b], xyz_stage.p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost,
-                         stream));
-      CK(cudaEventRecord(ev[b], stream));
+      CK(cudaEventRecord(ev_pack[b], stream));
+      CK(cudaStreamWaitEvent(cstream, ev_pack[b], 0));
+      CK(cudaMemcpyAsync(pinned[b], fstage[b].p, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost,
+                         cstream));
+      CK(cudaEventRecord(ev[b], cstream));
       for (auto &v : i_f) ++v;
       for (auto &v : t) v += par.spf * ff.dt;
-      if (pending >= 0) {
-        CK(cudaEventSynchronize(ev[pending]));
-        if (fn && fn(user, pend_if, pend_t, pinned[pending] + 3 * (size_t)d0.bead_off, d0.n))
-          throw Error(ST_IO, "frame callback failed");
-      }
+      if (pending >= 0) deliver(pending);
       pending = b;
       pend_if = i_f[0];
       pend_t = t[0];
     }
     if (pending >= 0) {
-      CK(cudaEventSynchronize(ev[pending]));
-      if (fn && fn(user, pend_if, pend_t, pinned[pending] + 3 * (size_t)d0.bead_off, d0.n))
-        throw Error(ST_IO, "frame callback failed");
+      deliver(pending);
       std::memcpy(hxyz.data(), pinned[pending], sizeof(float) * 3 * nb);
     }
     sync_and_check();
