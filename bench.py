@@ -246,7 +246,8 @@ def engine_arm(args, ws, rank, local):
     torch.cuda.set_device(local)
     sizes = replica_sizes(args.replicas)
     seeds = np.arange(args.replicas, dtype=np.uint64) + 1 + 100000 * rank
-    b = Batch(PARAMS, sizes, seeds=seeds)
+    params = PARAMS + ("pair_kernel %d\n" % args.pair_kernel if args.pair_kernel is not None else "")
+    b = Batch(params, sizes, seeds=seeds)
     b.generate_initial_condition()
     tune = b.autotune(reps=3) if not args.no_tune else None  # per size class, untimed
     total = int(sizes.sum())
@@ -320,6 +321,7 @@ def engine_arm(args, ws, rank, local):
                        "l2": "state (~%d MB) larger than the 129 MB L2" % (total * 100 // 2**20),
                        "parallelism": "replicas per GPU (no collective)",
                        "autotune": None if tune is None else {
+                           "pair_kernel": tune.get("pair_kernel"),
                            "tile": tune["tile"],
                            "cell_side_by_class": [[c["n_min"], c["n_max"], c["cell_side"]]
                                                   for c in tune["classes"]]}},
@@ -580,6 +582,8 @@ def main():
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
+    ap.add_argument("--pair-kernel", type=int, default=None,
+                    help="engine pair kernel (parameter pair_kernel); default: the engine's")
     ap.add_argument("--surrogate", action="store_true",
                     help="measure the surrogate on the c3/c4 protocol instead of the engine")
     ap.add_argument("--sur-profile", action="store_true",

@@ -149,10 +149,12 @@ int ccpgpu_stream_handle(ccpgpu_sim *h, void **stream);
  * [6] observe. Leaves the simulation state advanced by reps steps. */
 int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n);
 
-/* Autotuner (no reference counterpart): per size class of the batch (bead
- * counts in [2^k, 2^(k+1))) it times cell sides of 1, 0.75, 0.625, 0.55 and 0.5
- * times the largest cutoff (the last four with the 5x5x5 stencil), keeps the
- * fastest per class, then picks the per-bead tile size (64, 128, 256). Each
+/* Autotuner (no reference counterpart): for each half-shell pair kernel (2:
+ * one cell grid; 4: A beads and the others in separate grids) and per size
+ * class of the batch (bead counts in [2^k, 2^(k+1))) it times cell sides of 1,
+ * 0.75, 0.625, 0.55 and 0.5 times the largest cutoff (the last four with the
+ * 5x5x5 stencil), keeps the fastest per class, keeps the faster kernel, then
+ * picks the per-bead tile size (64, 128, 256). Requires pair_kernel 2 or 4. Each
  * candidate runs reps steps; positions, time and the noise counter are
  * restored afterwards. report receives a NUL-terminated JSON summary (size in
  * *len; CCPGPU_ERR_IO when cap is too small, after tuning). */

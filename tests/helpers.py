@@ -36,22 +36,27 @@ def force_errors(f_gpu, f_ref, absum):
     return rel, scaled
 
 
-def at_cutoff(x, fl, lbs, ff, tol=1e-5):
-    """Beads with an attractive (A-A) pair or a lamina-binding site within tol
-    of its cutoff. The baseline force field's truncated Lennard-Jones force
-    jumps there, so FP32 and FP64 distances may fall on opposite sides of the
-    cutoff and the two forces differ by the jump; such beads are checked
-    against the jump's size instead."""
+def at_cutoff(x, fl, lbs, ff, tol=1e-6):
+    """Beads with a pair or a lamina-binding site within tol of its cutoff
+    (A-A pairs at rc_att, other pairs at rc_rep). A truncated force jumps at
+    its cutoff, and FP32 and FP64 distances can fall on opposite sides of it
+    (tol covers a few FP32 ulps of the distance), so the two forces differ by
+    the jump there: the baseline Lennard-Jones at 2.5 sigma (~0.02), and the
+    Wang-Frenkel at the FP32 cutoff 1.154701, 4.6e-7 beyond its zero at
+    2/sqrt(3) (~1e-5; ccp's relaxation leaves many pairs exactly there).
+    Such beads are checked against the jump's size instead."""
     from scipy.spatial import cKDTree
 
     x = np.asarray(x, np.float64)
+    fl = np.asarray(fl)
     hit = np.zeros(len(x), bool)
-    a = np.flatnonzero(fl & 1)
-    if len(a) > 1:
-        t = cKDTree(x[a])
-        for i, j in t.query_pairs(ff["rc_att"] + tol, output_type="ndarray"):
-            if abs(np.linalg.norm(x[a[i]] - x[a[j]]) - ff["rc_att"]) < tol:
-                hit[a[i]] = hit[a[j]] = True
+    t = cKDTree(x)
+    rmax = max(ff["rc_att"], ff["rc_rep"]) + tol
+    for i, j in t.query_pairs(rmax, output_type="ndarray"):
+        aa = (fl[i] & 1) and (fl[j] & 1)
+        rc = ff["rc_att"] if aa else ff["rc_rep"]
+        if abs(np.linalg.norm(x[i] - x[j]) - rc) < tol:
+            hit[i] = hit[j] = True
     lad = np.flatnonzero(fl & 2)
     if len(lad) and len(lbs):
         t = cKDTree(np.asarray(lbs, np.float64).reshape(-1, 3))

@@ -79,6 +79,9 @@ struct SysDesc {
   int32_t nbins, map_len, copy_len, n_copies;
   int32_t sys_index;
   int32_t reach;  // neighbour cells per axis (1: csl >= cutoff, 2: csl >= cutoff / 2)
+  // typed layout: the cells of the non-A beads start cls_cells after those of
+  // the A beads (cps^3); 0: one grid for all beads
+  int32_t cls_cells;
 };
 
 // ---------------------------------------------------------------- Philox

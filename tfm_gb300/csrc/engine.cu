@@ -154,6 +154,7 @@ struct Engine {
       d.cps = 2 * (int)std::ceil(g.d_m / p.cell_side);
       if (d.cps < 2) d.cps = 2;
       d.cell_off = nc;
+      d.cls_cells = typed() ? d.cps * d.cps * d.cps : 0;
       d.R_n = g.R_n;
       d.R_o = g.R_o;
       d.R_b = g.R_b;
@@ -206,7 +207,7 @@ struct Engine {
       map_total += (int64_t)d.nbins * (d.nbins + 1) / 2;
       hsys[s] = d;
       nb += q.n;
-      nc += d.cps * d.cps * d.cps;
+      nc += (typed() ? 2 : 1) * d.cps * d.cps * d.cps;
       nl += q.n_lbs;
     }
     need_cut = std::max({ff.rc_att, ff.rc_rep, ff.rc_icg, p.contact_cutoff, ff.mis});
@@ -403,9 +404,47 @@ struct Engine {
     kcount += 1;
   }
 
+  // Typed layout (pair_kernel 4): A beads and the others sorted into separate
+  // cell grids of each system.
+  bool typed() const { return par.pair_kernel == 4; }
+
+  // Stencil reaches of the typed pair kernel for MODE when every system has
+  // the same (A-A reach * 4 + other reach), else 0.
+  template <int MODE>
+  int typed_reaches() const {
+    const float rhh = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_att;
+    const float rx = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_rep;
+    int key = -1;
+    for (const auto &d : hsys) {
+      int k = (d.csl >= rhh ? 1 : 2) * 4 + (d.csl >= rx ? 1 : 2);
+      if (key >= 0 && k != key) return 0;
+      key = k;
+    }
+    return key < 0 ? 0 : key;
+  }
+
   template <int MODE>
   void launch_pair() {
-    if (par.pair_kernel == 0)
+    const unsigned nt = (unsigned)htiles.size();
+    if (par.pair_kernel == 4) {
+      switch (typed_reaches<MODE>()) {
+        case 2 * 4 + 1:
+          k_pair_typed<MODE, 2, 1><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+          break;
+        case 1 * 4 + 1:
+          k_pair_typed<MODE, 1, 1><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+          break;
+        case 2 * 4 + 2:
+          k_pair_typed<MODE, 2, 2><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+          break;
+        default:  // systems gridded differently: each system's own reaches
+          k_pair_typed<MODE, 0, 0><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+      }
+    } else if (par.pair_kernel == 0)
       k_pair<MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
                                                                   start.p, fs.p);
     else if (par.pair_kernel == 3 && par.reach == 2)
@@ -561,7 +600,8 @@ struct Engine {
       d.cps = std::max(2, 2 * (int)std::ceil(geo[s].d_m / csl[s]));
       d.cell_off = nc;
       d.reach = (csl[s] >= need_cut) ? 1 : 2;
-      nc += d.cps * d.cps * d.cps;
+      d.cls_cells = typed() ? d.cps * d.cps * d.cps : 0;
+      nc += (typed() ? 2 : 1) * d.cps * d.cps * d.cps;
     }
     build_tiles();
     nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
@@ -600,14 +640,17 @@ struct Engine {
     return ms / reps;
   }
 
-  // Autotuner: per size class (bead counts in [2^k, 2^(k+1))) the cell side
+  // Autotuner: for each half-shell pair kernel (2: one grid; 4: the typed
+  // layout), per size class (bead counts in [2^k, 2^(k+1))) the cell side
   // factor f (cell side = f * largest cutoff; f >= 1 uses the 3x3x3 stencil,
-  // f in [0.5, 1) the 5x5x5 one), then the per-bead tile size. Each candidate
-  // is timed over `reps` steps; the state, time and noise counter are restored
-  // afterwards, so tuning does not change the trajectory. Returns a JSON report.
+  // f in [0.5, 1) the 5x5x5 one); then the faster kernel with its cell sides,
+  // then the per-bead tile size. Each candidate is timed over `reps` steps;
+  // the state, time and noise counter are restored afterwards, so tuning does
+  // not change the trajectory. Returns a JSON report.
   std::string autotune(int reps) {
     if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
-    if (par.pair_kernel != 2) throw Error(ST_ARG, "autotune needs the half-shell pair kernel");
+    if (par.pair_kernel != 2 && par.pair_kernel != 4)
+      throw Error(ST_ARG, "autotune needs a half-shell pair kernel");
     download_positions();
     std::vector<float> saved_xyz = hxyz;
     uint64_t saved_step = step;
@@ -620,38 +663,58 @@ struct Engine {
       cls[s] = k;
       members[k].push_back(s);
     }
-    std::vector<float> csl(ns);
-    for (int s = 0; s < ns; ++s) csl[s] = hsys[s].csl;
+    std::vector<float> csl0(ns);
+    for (int s = 0; s < ns; ++s) csl0[s] = hsys[s].csl;
     const float factors[] = {1.0f, 0.5f, 0.55f, 0.625f, 0.75f};
-    std::ostringstream rep;
-    rep << "{\"classes\": [";
-    bool first = true;
-    for (auto &kv : members) {
-      double best = 1e30;
-      float best_f = 1.0f;
-      std::ostringstream tried;
-      for (float f : factors) {
-        for (int s : kv.second) csl[s] = f * need_cut;
-        regrid(csl, tile);
-        double ms = time_steps(reps);
-        tried << (tried.tellp() > 0 ? ", " : "") << "[" << f << ", " << ms << "]";
-        if (ms < best) {
-          best = ms;
-          best_f = f;
+    struct Choice {
+      int kernel;
+      double ms;
+      std::vector<float> csl;
+      std::string classes;
+    };
+    std::vector<Choice> choices;
+    for (int kernel : {par.pair_kernel, par.pair_kernel == 2 ? 4 : 2}) {
+      par.pair_kernel = kernel;
+      std::vector<float> csl = csl0;
+      std::ostringstream rep;
+      bool first = true;
+      double last = 1e30;
+      for (auto &kv : members) {
+        double best = 1e30;
+        float best_f = 1.0f;
+        std::ostringstream tried;
+        for (float f : factors) {
+          for (int s : kv.second) csl[s] = f * need_cut;
+          regrid(csl, tile);
+          double ms = time_steps(reps);
+          tried << (tried.tellp() > 0 ? ", " : "") << "[" << f << ", " << ms << "]";
+          if (ms < best) {
+            best = ms;
+            best_f = f;
+          }
         }
+        for (int s : kv.second) csl[s] = best_f * need_cut;
+        last = best;
+        int nmin = 1 << 30, nmax = 0;
+        for (int s : kv.second) {
+          nmin = std::min(nmin, hsys[s].n);
+          nmax = std::max(nmax, hsys[s].n);
+        }
+        rep << (first ? "" : ", ") << "{\"n_min\": " << nmin << ", \"n_max\": " << nmax
+            << ", \"systems\": " << kv.second.size() << ", \"cell_side\": " << best_f * need_cut
+            << ", \"reach\": " << (best_f >= 1.0f ? 1 : 2) << ", \"tried\": [" << tried.str()
+            << "]}";
+        first = false;
       }
-      for (int s : kv.second) csl[s] = best_f * need_cut;
-      int nmin = 1 << 30, nmax = 0;
-      for (int s : kv.second) {
-        nmin = std::min(nmin, hsys[s].n);
-        nmax = std::max(nmax, hsys[s].n);
-      }
-      rep << (first ? "" : ", ") << "{\"n_min\": " << nmin << ", \"n_max\": " << nmax
-          << ", \"systems\": " << kv.second.size() << ", \"cell_side\": " << best_f * need_cut
-          << ", \"reach\": " << (best_f >= 1.0f ? 1 : 2) << ", \"tried\": [" << tried.str()
-          << "]}";
-      first = false;
+      choices.push_back(Choice{kernel, last, csl, rep.str()});
     }
+    const Choice &ch = (choices[1].ms < choices[0].ms) ? choices[1] : choices[0];
+    par.pair_kernel = ch.kernel;
+    std::vector<float> csl = ch.csl;
+    std::ostringstream rep;
+    rep << "{\"pair_kernel\": " << ch.kernel << ", \"kernels_tried\": [[" << choices[0].kernel
+        << ", " << choices[0].ms << "], [" << choices[1].kernel << ", " << choices[1].ms
+        << "]], \"classes\": [" << ch.classes;
     double best = 1e30;
     int best_tile = tile;
     std::ostringstream tt;

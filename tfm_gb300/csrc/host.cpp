@@ -210,8 +210,10 @@ Params parse_params(const std::string &text) {
   p.lad_fraction = pm.get<float>("lad_fraction", 0.1f);
   p.mean_block = pm.get<float>("mean_block_length", 16.0f);
   p.sequence_file = pm.get<std::string>("sequence_file", p.sequence_file);
-  p.pair_kernel = pm.get<int>("pair_kernel", 2);
-  if (!(p.pair_kernel >= 0 && p.pair_kernel <= 3)) fail("pair_kernel out of range");
+  // the typed layout pays off when the repulsive cutoff is below the cell side
+  // (baseline cells of 1.25 sigma); ccp's cells of aco = 2 sigma gain nothing
+  p.pair_kernel = pm.get<int>("pair_kernel", p.preset == PRESET_BASELINE ? 4 : 2);
+  if (!(p.pair_kernel >= 0 && p.pair_kernel <= 4)) fail("pair_kernel out of range");
   if (!(p.n_chains >= 1 && (uint32_t)p.n_chains <= p.N)) fail("number_of_chains out of range");
   if (!(p.contact_cutoff > 0.0f)) fail("contact_cutoff out of range");
   if (p.contact_bins < 0) fail("contact_bins out of range");

@@ -78,6 +78,13 @@ __device__ __forceinline__ int cell_linear(CellXYZ c, const SysDesc &s) {
   return s.cell_off + (c.z * s.cps + c.y) * s.cps + c.x;
 }
 
+// Cell of a bead in the sort: the A beads (BF_HET) use the system's first
+// grid, the other beads the second one when the layout is typed.
+__device__ __forceinline__ int bead_cell(float4 p, const SysDesc &s, bool &esc) {
+  int c = cell_linear(cell_of(p, s, esc), s);
+  return (wbits(p) & BF_HET) ? c : c + s.cls_cells;
+}
+
 __device__ __forceinline__ void set_err(int *err, int code) {
   if (err[code] == 0) atomicExch(&err[code], 1);
 }
@@ -274,7 +281,7 @@ __global__ void k_count(const Tile *__restrict__ tiles, const SysDesc *__restric
   if (i >= s.bead_off + s.n) return;
   bool esc = false;
   float4 p = pos[i];
-  int c = cell_linear(cell_of(p, s, esc), s);
+  int c = bead_cell(p, s, esc);
   rank[i] = atomicAdd(&counts[c], 1u);
   if (esc) set_err(err, ERR_ESCAPE);
 }
@@ -407,7 +414,7 @@ __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restr
   if (fs_clear) fs_clear[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // for the half-shell pass
   bool esc = false;
   float4 p = src[i];
-  int c = cell_linear(cell_of(p, s, esc), s);
+  int c = bead_cell(p, s, esc);
   uint32_t slot = start[c] + rank[i];
   if (slot < (uint32_t)s.bead_off || slot >= (uint32_t)end) {
     set_err(err, ERR_SLOT);
@@ -528,6 +535,46 @@ __device__ __forceinline__ void half_pair(float4 p, uint32_t wi, const float4 *_
   atomicAdd(&fs[k], make_float4(-fx, -fy, -fz, 0.0f));
 }
 
+// half_pair on a candidate already loaded, with an early exit for the common
+// case: most candidates lie beyond the largest cutoff (rc2_max = its square),
+// so the type and chain-neighbour tests run only for the rest.
+template <int MODE>
+__device__ __forceinline__ void half_pair_q(float4 p, uint32_t wi, float4 q, uint32_t k,
+                                            const ForceField &ff, float rc2_max, float3 &acc,
+                                            float4 *__restrict__ fs) {
+  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  if (d2 > rc2_max) return;
+  uint32_t wj = wbits(q);
+  bool hh = (wi & wj & BF_HET) != 0u;
+  if (MODE != MODE_ICG) {
+    float rc = hh ? ff.rc_att : ff.rc_rep;
+    if (d2 > rc * rc) return;
+  }
+  int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
+  if ((unsigned)(gi - gj + 1) <= 2u) return;
+  float cf = pair_coef<MODE>(d2, hh, ff);
+  float fx = cf * dx, fy = cf * dy, fz = cf * dz;
+  acc.x += fx;
+  acc.y += fy;
+  acc.z += fz;
+  atomicAdd(&fs[k], make_float4(-fx, -fy, -fz, 0.0f));
+}
+
+// Candidates [b, e) of one row range, two loads in flight per iteration.
+template <int MODE>
+__device__ __forceinline__ void half_range(float4 p, uint32_t wi, const float4 *__restrict__ sorted,
+                                           uint32_t b, uint32_t e, const ForceField &ff,
+                                           float rc2_max, float3 &acc, float4 *__restrict__ fs) {
+  uint32_t k = b;
+  for (; k + 1 < e; k += 2) {
+    float4 q0 = __ldg(&sorted[k]), q1 = __ldg(&sorted[k + 1]);
+    half_pair_q<MODE>(p, wi, q0, k, ff, rc2_max, acc, fs);
+    half_pair_q<MODE>(p, wi, q1, k + 1, ff, rc2_max, acc, fs);
+  }
+  if (k < e) half_pair_q<MODE>(p, wi, __ldg(&sorted[k]), k, ff, rc2_max, acc, fs);
+}
+
 // REACH = 1: cells of side >= the largest cutoff, 3x3x3 neighbourhood.
 // REACH = 2: cells of side >= half of it, 5x5x5 neighbourhood: the candidate
 // volume drops from 27 to 15.6 cutoff-cubes (x0.58) at the price of 13 instead
@@ -549,12 +596,14 @@ __global__ void __launch_bounds__(256)
   CellXYZ c = cell_of(p, s, esc);
   const int cps = s.cps;
   const int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+  const float rc_max = (MODE == MODE_ICG) ? ff.rc_icg : fmaxf(ff.rc_att, ff.rc_rep);
+  const float rc2_max = rc_max * rc_max;
   float3 acc = make_float3(0.0f, 0.0f, 0.0f);
   // own cell after i, then the +x cells
   {
     int row = s.cell_off + (c.z * cps + c.y) * cps;
     uint32_t e = __ldg(&start[row + x1 + 1]);
-    for (uint32_t k = slot + 1; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
+    half_range<MODE>(p, wi, sorted, slot + 1, e, ff, rc2_max, acc, fs);
   }
   // the +y rows of this layer, then all rows of the +z layers
   const int NR = R + R * (2 * R + 1);
@@ -572,7 +621,122 @@ __global__ void __launch_bounds__(256)
     if (y < 0 || y >= cps || z >= cps) continue;
     int row = s.cell_off + (z * cps + y) * cps;
     uint32_t b = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]);
-    for (uint32_t k = b; k < e; ++k) half_pair<MODE>(p, wi, sorted, k, ff, acc, fs);
+    half_range<MODE>(p, wi, sorted, b, e, ff, rc2_max, acc, fs);
+  }
+  atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
+}
+
+// Pair term of the typed kernel, the pair's class (A-A or not) known from
+// the grid it was found in; rc2 = the square of that class's cutoff.
+template <int MODE, bool HH>
+__device__ __forceinline__ void typed_pair(float4 p, uint32_t wi, float4 q, uint32_t k,
+                                           const ForceField &ff, float rc2, float3 &acc,
+                                           float4 *__restrict__ fs) {
+  float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  if (d2 > rc2) return;
+  int gi = (int)(wi >> BF_BITS), gj = (int)(wbits(q) >> BF_BITS);
+  if ((unsigned)(gi - gj + 1) <= 2u) return;
+  float cf = pair_coef<MODE>(d2, HH, ff);
+  float fx = cf * dx, fy = cf * dy, fz = cf * dz;
+  acc.x += fx;
+  acc.y += fy;
+  acc.z += fz;
+  atomicAdd(&fs[k], make_float4(-fx, -fy, -fz, 0.0f));
+}
+
+template <int MODE, bool HH>
+__device__ __forceinline__ void typed_range(float4 p, uint32_t wi, const float4 *__restrict__ sorted,
+                                            uint32_t b, uint32_t e, const ForceField &ff,
+                                            float rc2, float3 &acc, float4 *__restrict__ fs) {
+  uint32_t k = b;
+  for (; k + 1 < e; k += 2) {
+    float4 q0 = __ldg(&sorted[k]), q1 = __ldg(&sorted[k + 1]);
+    typed_pair<MODE, HH>(p, wi, q0, k, ff, rc2, acc, fs);
+    typed_pair<MODE, HH>(p, wi, q1, k + 1, ff, rc2, acc, fs);
+  }
+  if (k < e) typed_pair<MODE, HH>(p, wi, __ldg(&sorted[k]), k, ff, rc2, acc, fs);
+}
+
+// Forward half of the (2R+1)^3 stencil of cell c in the grid starting at cell
+// g0: the beads after `slot` in its own cell and the +x cells, the +y rows of
+// its layer, and every row of the +z layers.
+template <int MODE, bool HH>
+__device__ __forceinline__ void typed_half(float4 p, uint32_t wi, int slot, CellXYZ c, int g0,
+                                           int cps, int R, const float4 *__restrict__ sorted,
+                                           const uint32_t *__restrict__ start,
+                                           const ForceField &ff, float rc2, float3 &acc,
+                                           float4 *__restrict__ fs) {
+  const int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+  {
+    int row = g0 + (c.z * cps + c.y) * cps;
+    typed_range<MODE, HH>(p, wi, sorted, slot + 1, __ldg(&start[row + x1 + 1]), ff, rc2, acc, fs);
+  }
+  const int NR = R + R * (2 * R + 1);
+#pragma unroll 1
+  for (int r = 0; r < NR; ++r) {
+    int y, z;
+    if (r < R) {
+      y = c.y + 1 + r;
+      z = c.z;
+    } else {
+      int q = r - R;
+      y = c.y - R + q % (2 * R + 1);
+      z = c.z + 1 + q / (2 * R + 1);
+    }
+    if (y < 0 || y >= cps || z >= cps) continue;
+    int row = g0 + (z * cps + y) * cps;
+    typed_range<MODE, HH>(p, wi, sorted, __ldg(&start[row + x0]), __ldg(&start[row + x1 + 1]), ff,
+                          rc2, acc, fs);
+  }
+}
+
+// Half-shell pair kernel over the typed layout (SysDesc::cls_cells > 0): in
+// every system the A beads are sorted by cell first, then the other beads,
+// each class in its own grid. Only A-A pairs interact beyond the repulsive
+// cutoff, so
+//   an A bead visits A-A pairs over the forward half of the RHH stencil of
+//     the A grid and A-other pairs over the full RX stencil of the other grid;
+//   another bead visits other-other pairs over the forward half of the RX
+//     stencil of the other grid.
+// Every unordered pair is visited once, the class of each pair is known from
+// its grid, warps hold one class (but at most one per system), and the
+// non-A beads scan only the small stencil. RHH / RX = 0: from the system's
+// cell side (1 when it is at least the cutoff, else 2).
+template <int MODE, int RHH, int RX>
+__global__ void __launch_bounds__(256)
+    k_pair_typed(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
+                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+                 float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  int slot = t.begin + threadIdx.x;
+  if (slot >= s.bead_off + s.n) return;
+  float4 p = sorted[slot];
+  uint32_t wi = wbits(p);
+  bool esc = false;
+  CellXYZ c = cell_of(p, s, esc);
+  const int cps = s.cps;
+  const float rc_hh = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_att;
+  const float rc_x = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_rep;
+  const int rhh = (RHH > 0) ? RHH : (s.csl >= rc_hh ? 1 : 2);
+  const int rx = (RX > 0) ? RX : (s.csl >= rc_x ? 1 : 2);
+  const int gA = s.cell_off, gX = s.cell_off + s.cls_cells;
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+  if (wi & BF_HET) {
+    typed_half<MODE, true>(p, wi, slot, c, gA, cps, rhh, sorted, start, ff, rc_hh * rc_hh, acc, fs);
+    const int x0 = max(c.x - rx, 0), x1 = min(c.x + rx, cps - 1);
+    const float rc2 = rc_x * rc_x;
+#pragma unroll 1
+    for (int z = max(c.z - rx, 0); z <= min(c.z + rx, cps - 1); ++z)
+#pragma unroll 1
+      for (int y = max(c.y - rx, 0); y <= min(c.y + rx, cps - 1); ++y) {
+        int row = gX + (z * cps + y) * cps;
+        typed_range<MODE, false>(p, wi, sorted, __ldg(&start[row + x0]),
+                                 __ldg(&start[row + x1 + 1]), ff, rc2, acc, fs);
+      }
+  } else {
+    typed_half<MODE, false>(p, wi, slot, c, gX, cps, rx, sorted, start, ff, rc_x * rc_x, acc, fs);
   }
   atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
 }
@@ -855,7 +1019,7 @@ __global__ void __launch_bounds__(256)
 
   // pair force of this bead from the cell-ordered pass
   bool esc = false;
-  int c_old = cell_linear(cell_of(xi, s, esc), s);
+  int c_old = bead_cell(xi, s, esc);
   uint32_t slot = start[c_old] + rank[i];
   float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end)
@@ -908,7 +1072,7 @@ __global__ void __launch_bounds__(256)
   }
   if (!(isfinite(out.x) && isfinite(out.y) && isfinite(out.z))) set_err(err, ERR_NAN);
   bool esc2 = false;
-  int c_new = cell_linear(cell_of(out, s, esc2), s);
+  int c_new = bead_cell(out, s, esc2);
   rank[i] = atomicAdd(&counts[c_new], 1u);
   if (esc2) set_err(err, ERR_ESCAPE);
 }
@@ -930,7 +1094,7 @@ __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__r
   if (i >= end) return;
   float4 xi = pos[i];
   bool esc = false;
-  int c = cell_linear(cell_of(xi, s, esc), s);
+  int c = bead_cell(xi, s, esc);
   uint32_t slot = start[c] + rank[i];
   float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end) fp = fs[slot];
@@ -1011,9 +1175,11 @@ __global__ void __launch_bounds__(256)
     const int cps = s.cps;
     const int R = (REACH > 0) ? REACH : s.reach;  // 0: the system's own reach
     int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+    const int ngrid = s.cls_cells ? 2 : 1;  // typed layout: both grids
+    for (int g = 0; g < ngrid; ++g)
     for (int z = max(c.z - R, 0); z <= min(c.z + R, cps - 1); ++z)
       for (int y = max(c.y - R, 0); y <= min(c.y + R, cps - 1); ++y) {
-        int row = s.cell_off + (z * cps + y) * cps;
+        int row = s.cell_off + g * s.cls_cells + (z * cps + y) * cps;
         uint32_t b = start[row + x0], e = start[row + x1 + 1];
         for (uint32_t k = b; k < e; ++k) {
           float4 q = sorted[k];
