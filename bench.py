@@ -44,8 +44,9 @@ HEUN_PER_STEP = 100
 B_ALG = 192.0  # algorithmic HBM bytes per bead-step of a Heun step (2 force evaluations)
 PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4 force
 # DRAM bytes per bead of one pair launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on this workload: profiles/k_pair_half_c2.md
-PAIR_TRAFFIC_PER_BEAD = 47.1
+# dram__bytes_write.sum) on this workload with the typed pair kernel the
+# autotuner keeps: profiles/k_pair_typed_c2.md
+PAIR_TRAFFIC_PER_BEAD = 58.3
 METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
 
 
