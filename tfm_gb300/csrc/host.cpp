@@ -220,9 +220,10 @@ Params parse_params(const std::string &text) {
   if (!(p.lad_fraction >= 0.0f && p.lad_fraction <= 1.0f)) fail("lad_fraction out of range");
   if (!(p.mean_block >= 1.0f)) fail("mean_block_length out of range");
   float need = std::max({p.ff.rc_att, p.ff.rc_rep, p.ff.rc_icg, p.contact_cutoff, p.ff.mis});
-  // ccp: its grid of side aco (chrsim.cu:425); baseline: cells of half the
-  // largest cutoff with the 5x5x5 half-shell stencil (measured fastest on GB300)
-  float def_cs = (p.preset == PRESET_CCP) ? CCP_ACO : (p.pair_kernel >= 2 ? 0.5f * need : need);
+  // cells of half the largest cutoff with the 5x5x5 half-shell stencil: for
+  // ccp (whose own grid has side aco = 2, chrsim.cu:425) 15-20 % faster per
+  // step than cells of aco on one system of 8192-99000 beads (GB300)
+  float def_cs = (p.pair_kernel >= 2) ? 0.5f * need : need;
   p.cell_side = pm.get<float>("cell_side", def_cs);
   // cells of at least the largest cutoff use the 3x3x3 neighbourhood; cells of
   // at least half of it the 5x5x5 one (half-shell pair kernel only)
