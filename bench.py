@@ -118,34 +118,21 @@ class Clocks:
 
 
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
+    from tfm_gb300 import replicas
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    return ws, rank, local
+    return replicas.init()
 
 
 def barrier(ws):
-    if ws > 1:
-        import torch.distributed as dist
+    from tfm_gb300 import replicas
 
-        dist.barrier()
+    replicas.barrier(ws)
 
 
 def max_over_ranks(v, ws):
-    if ws == 1:
-        return v
-    import torch
-    import torch.distributed as dist
+    from tfm_gb300 import replicas
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return replicas.max_over_ranks(v, ws)
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -240,13 +227,14 @@ def engine_arm(args, ws, rank, local):
     import torch
 
     from tfm_gb300 import build as eb
+    from tfm_gb300 import replicas
 
     eb.build()
     from tfm_gb300.ccpgpu import Batch
 
     torch.cuda.set_device(local)
     sizes = replica_sizes(args.replicas)
-    seeds = np.arange(args.replicas, dtype=np.uint64) + 1 + 100000 * rank
+    seeds = replicas.replica_seeds(args.replicas, rank)  # disjoint per rank
     params = PARAMS + ("pair_kernel %d\n" % args.pair_kernel if args.pair_kernel is not None else "")
     b = Batch(params, sizes, seeds=seeds)
     b.generate_initial_condition()
@@ -279,7 +267,7 @@ def engine_arm(args, ws, rank, local):
     ms = ev0.elapsed_time(ev1)
     launches = b.kernel_count() - k0
     ms = max_over_ranks(ms, ws)
-    value = ws * total * HEUN_PER_STEP * args.steps / (ms / 1000.0)
+    value = replicas.whole_job_rate(total * HEUN_PER_STEP * args.steps, ws, ms / 1000.0)
     ms_step = ms / args.steps
 
     # dominant kernel (pair) timed live with CUDA events on the engine stream
@@ -300,7 +288,7 @@ def engine_arm(args, ws, rank, local):
         x = b.positions()  # D2H of the step's result
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, ws)
-    e2e_val = ws * total * HEUN_PER_STEP * args.steps / e2e_s
+    e2e_val = replicas.whole_job_rate(total * HEUN_PER_STEP * args.steps, ws, e2e_s)
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -608,10 +596,9 @@ def main():
         reference_arm(args, ws, rank)
     else:
         engine_arm(args, ws, rank, local)
-    if ws > 1:
-        import torch.distributed as dist
+    from tfm_gb300 import replicas
 
-        dist.destroy_process_group()
+    replicas.finalize(ws)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,76 @@
+"""Several GPUs of one node: one process per GPU, each advancing its own batch
+of replicas. The replicas are independent simulations, so no data crosses
+ranks; the only collectives are a barrier around a timed region and the
+maximum of the ranks' timings (the whole job is as slow as its slowest rank).
+
+Each rank draws its replicas' seeds from its own disjoint range, so an N-rank
+job simulates N distinct ensembles (weak scaling: the work per GPU is fixed).
+"""
+import os
+
+import numpy as np
+
+SEED_STRIDE = 100000  # seeds of rank r: r * SEED_STRIDE + 1 ... r * SEED_STRIDE + n
+
+
+def world():
+    """(world size, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def init(backend=None):
+    """Joins the process group when the job has more than one rank: NCCL on
+    GPUs (one device per local rank), gloo otherwise. Returns world()."""
+    ws, rank, local = world()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def finalize(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+def replica_seeds(n_replicas, rank):
+    """Seeds of one rank's replicas; disjoint between ranks."""
+    if not 0 < n_replicas < SEED_STRIDE:
+        raise ValueError("replicas per rank must be in [1, %d)" % SEED_STRIDE)
+    return np.arange(n_replicas, dtype=np.uint64) + 1 + SEED_STRIDE * rank
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    """The largest v over all ranks (every rank receives it)."""
+    if ws == 1:
+        return float(v)
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, ws, seconds):
+    """Units processed by all ranks per second of the slowest rank's time."""
+    return ws * float(units_per_rank) / float(seconds)
