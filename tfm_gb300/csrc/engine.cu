@@ -505,13 +505,13 @@ struct Engine {
   void launch_contacts_args(const ContactArgs &a) {
     const int r = uniform_reach();
     if (r == 1)
-      k_contacts<1><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+      k_contacts_half<1><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
                                                                     start.p, a);
     else if (r == 2)
-      k_contacts<2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+      k_contacts_half<2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
                                                                     start.p, a);
     else
-      k_contacts<0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
+      k_contacts_half<0><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, sorted.p,
                                                                     start.p, a);
     kcount += 1;
   }

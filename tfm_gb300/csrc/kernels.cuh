@@ -1147,65 +1147,122 @@ struct ContactArgs {
   unsigned long long *overlaps;  // per-system overlap count
 };
 
-// One pass over unordered bead pairs (i < j) within the contact cutoff of the
+
+
+// One unordered pair (i, j) of the half-shell contact pass, in either order:
+// the pair is counted for the bead with the lower index, as the full-stencil
+// pass counts it (gj > gi).
+struct ContactBead {
+  int g, copy, lc, bin, ch;
+  bool mapped;
+};
+
+__device__ __forceinline__ ContactBead contact_bead(int g, const SysDesc &s, const ContactArgs &a) {
+  ContactBead b;
+  b.g = g;
+  int l = g - s.bead_off;
+  b.copy = l / s.copy_len;
+  b.lc = l - b.copy * s.copy_len;
+  b.mapped = b.copy < s.n_copies && b.lc < s.map_len;
+  b.bin = b.mapped ? (int)(((long long)b.lc * s.nbins) / s.map_len) : 0;
+  b.ch = a.chain_of[g];
+  return b;
+}
+
+__device__ __forceinline__ void contact_pair(float4 p, const ContactBead &bi, float4 q,
+                                             const SysDesc &s, const ContactArgs &a,
+                                             unsigned long long &novl) {
+  int gj = (int)(wbits(q) >> BF_BITS);
+  int lo = min(bi.g, gj), hi = max(bi.g, gj);
+  if (a.do_overlap && hi - lo >= 2 && in_contact(p, q, a.mis)) ++novl;
+  if (!in_contact(p, q, a.cut)) return;
+  ContactBead bj = contact_bead(gj, s, a);
+  if (a.do_map && bi.mapped && bj.mapped && bi.copy == bj.copy) {
+    int bx = max(bi.bin, bj.bin), by = min(bi.bin, bj.bin);
+    long long idx = s.map_off + (long long)bx * (bx + 1) / 2 + by;
+    atomicAdd(&a.map[idx], bx == by ? 2 : 1);
+  }
+  if (a.do_ps && bj.ch == bi.ch) {
+    int sep = hi - lo;
+    if (sep <= a.chain_smax[bi.ch]) atomicAdd(&a.ps[a.chain_ps_off[bi.ch] + sep], 1);
+  }
+}
+
+// Forward half of the (2R+1)^3 stencil in the grid starting at cell g0 (the
+// own cell after `slot` and the +x cells, the +y rows, the +z layers), or
+// the full stencil (FULL) of that grid.
+template <bool FULL>
+__device__ __forceinline__ void contact_rows(float4 p, const ContactBead &bi, int slot, CellXYZ c,
+                                             int g0, int R, const SysDesc &s,
+                                             const float4 *__restrict__ sorted,
+                                             const uint32_t *__restrict__ start,
+                                             const ContactArgs &a, unsigned long long &novl) {
+  const int cps = s.cps;
+  const int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+  if (FULL) {
+    for (int z = max(c.z - R, 0); z <= min(c.z + R, cps - 1); ++z)
+      for (int y = max(c.y - R, 0); y <= min(c.y + R, cps - 1); ++y) {
+        int row = g0 + (z * cps + y) * cps;
+        for (uint32_t k = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]); k < e; ++k)
+          contact_pair(p, bi, __ldg(&sorted[k]), s, a, novl);
+      }
+    return;
+  }
+  {
+    int row = g0 + (c.z * cps + c.y) * cps;
+    for (uint32_t k = slot + 1, e = __ldg(&start[row + x1 + 1]); k < e; ++k)
+      contact_pair(p, bi, __ldg(&sorted[k]), s, a, novl);
+  }
+  const int NR = R + R * (2 * R + 1);
+  for (int r = 0; r < NR; ++r) {
+    int y, z;
+    if (r < R) {
+      y = c.y + 1 + r;
+      z = c.z;
+    } else {
+      int q = r - R;
+      y = c.y - R + q % (2 * R + 1);
+      z = c.z + 1 + q / (2 * R + 1);
+    }
+    if (y < 0 || y >= cps || z >= cps) continue;
+    int row = g0 + (z * cps + y) * cps;
+    for (uint32_t k = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]); k < e; ++k)
+      contact_pair(p, bi, __ldg(&sorted[k]), s, a, novl);
+  }
+}
+
+// One pass over unordered bead pairs within the contact cutoff of the
 // cell-ordered copy: binned contact map (calc_cm, chrana.cu:48-84), per-chain
 // contact counts by separation (the cp part of calc_sd_cp, chrana.cu:13-45) and
 // the overlap count of the initial-condition relaxation (chrsim.cu:805-820).
-// REACH as for the pair kernel (cells of side >= cutoff / REACH).
+// Every unordered pair is visited once, over half stencils: one grid, or the
+// typed layout's A-A half, A-other full and other-other half stencils (the
+// contact predicate is symmetric in i and j). REACH as for the pair kernel
+// (cells of side >= cutoff / REACH); 0: each system's own reach.
 template <int REACH = 1>
 __global__ void __launch_bounds__(256)
-    k_contacts(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
-               const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
-               ContactArgs a) {
+    k_contacts_half(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                    const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
+                    ContactArgs a) {
   Tile t = tiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
   int slot = t.begin + threadIdx.x;
   unsigned long long novl = 0;
   if (slot < s.bead_off + s.n) {
     float4 p = sorted[slot];
-    int gi = (int)(wbits(p) >> BF_BITS);
-    int li = gi - s.bead_off;
-    int copy_i = li / s.copy_len, lc_i = li - copy_i * s.copy_len;
-    bool mapped_i = a.do_map && copy_i < s.n_copies && lc_i < s.map_len;
-    int bin_i = mapped_i ? (int)(((long long)lc_i * s.nbins) / s.map_len) : 0;
-    int ch_i = a.chain_of[gi];
-    float mis2 = a.mis;
+    ContactBead bi = contact_bead((int)(wbits(p) >> BF_BITS), s, a);
+    bi.mapped = bi.mapped && a.do_map;
     bool esc = false;
     CellXYZ c = cell_of(p, s, esc);
-    const int cps = s.cps;
-    const int R = (REACH > 0) ? REACH : s.reach;  // 0: the system's own reach
-    int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
-    const int ngrid = s.cls_cells ? 2 : 1;  // typed layout: both grids
-    for (int g = 0; g < ngrid; ++g)
-    for (int z = max(c.z - R, 0); z <= min(c.z + R, cps - 1); ++z)
-      for (int y = max(c.y - R, 0); y <= min(c.y + R, cps - 1); ++y) {
-        int row = s.cell_off + g * s.cls_cells + (z * cps + y) * cps;
-        uint32_t b = start[row + x0], e = start[row + x1 + 1];
-        for (uint32_t k = b; k < e; ++k) {
-          float4 q = sorted[k];
-          int gj = (int)(wbits(q) >> BF_BITS);
-          if (gj <= gi) continue;
-          if (a.do_overlap && gj - gi >= 2 && in_contact(p, q, mis2)) ++novl;
-          if (!in_contact(p, q, a.cut)) continue;
-          if (mapped_i) {
-            int lj = gj - s.bead_off;
-            int copy_j = lj / s.copy_len, lc_j = lj - copy_j * s.copy_len;
-            if (copy_j == copy_i && lc_j < s.map_len) {
-              int bin_j = (int)(((long long)lc_j * s.nbins) / s.map_len);
-              int bx = max(bin_i, bin_j), by = min(bin_i, bin_j);
-              long long idx = s.map_off + (long long)bx * (bx + 1) / 2 + by;
-              atomicAdd(&a.map[idx], bx == by ? 2 : 1);
-            }
-          }
-          if (a.do_ps) {
-            int ch_j = a.chain_of[gj];
-            if (ch_j == ch_i) {
-              int sep = gj - gi;
-              if (sep <= a.chain_smax[ch_i]) atomicAdd(&a.ps[a.chain_ps_off[ch_i] + sep], 1);
-            }
-          }
-        }
-      }
+    const int R = (REACH > 0) ? REACH : s.reach;
+    if (s.cls_cells == 0) {
+      contact_rows<false>(p, bi, slot, c, s.cell_off, R, s, sorted, start, a, novl);
+    } else if (wbits(p) & BF_HET) {
+      contact_rows<false>(p, bi, slot, c, s.cell_off, R, s, sorted, start, a, novl);
+      contact_rows<true>(p, bi, slot, c, s.cell_off + s.cls_cells, R, s, sorted, start, a, novl);
+    } else {
+      contact_rows<false>(p, bi, slot, c, s.cell_off + s.cls_cells, R, s, sorted, start, a, novl);
+    }
   }
   if (a.do_overlap) {
 #pragma unroll
