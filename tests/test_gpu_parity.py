@@ -291,6 +291,27 @@ def test_trajectory_matches_oracle_1000_steps(engine_lib, orc):
     assert drift.max() < 2e-3
 
 
+def test_trajectory_baseline_matches_oracle_1000_steps(engine_lib, orc):
+    """The same for the baseline force field (Lennard-Jones A-A attraction,
+    WCA, lamina sites, the displacement cap) on its default typed pair
+    kernel: 1000 Heun steps vs the FP64 oracle, max |dr| < 2e-3 sigma."""
+    from tfm_gb300.ccpgpu import ChrSim
+
+    sim = ChrSim(baseline_params(1024), seed=4321)
+    assert "pair_kernel" not in baseline_params(1024)  # the preset's default (typed)
+    sim.generate_initial_condition()
+    x0, pt, lbs = sim.positions(), sim.types(), sim.lbs()
+    step0 = sim.info().step
+    sim.run_steps(1000)
+    xg = sim.positions().astype(np.float64)
+    fl = orc.flags_from_types(pt, [0], "baseline")
+    geo = orc.geo_vec(sim.system_info(0).nucleus_radius, csl=2.5)
+    x64 = orc.run(x0, fl, lbs, orc.baseline_ff(), geo, 4321, step0, 1000, prec=64)
+    drift = np.linalg.norm(xg - x64, axis=1)
+    print("baseline 1000-step drift: max %.3g  mean %.3g" % (drift.max(), drift.mean()))
+    assert drift.max() < 2e-3
+
+
 def test_batch_matches_single_systems(engine_lib):
     from tfm_gb300.ccpgpu import Batch, ChrSim
 
