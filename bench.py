@@ -187,6 +187,169 @@ def cpu_sample(sizes, seconds=12.0, prebuilt=None):
         "%d replicas (%d beads) x %d Heun steps, FP32" % (len(systems), beads, steps)
 
 
+# ------------------------------------------------- reference kernels on the GPU
+REF_CUBIN = os.path.join(ROOT, "oracle", "_ref", "ccp_ref.cubin")
+REF_NAMES = {  # entry names as ptxas reports them for oracle/ref/ref_kernels.cu
+    "init_ps": "_ZN3mmc7init_psEjP24curandStatePhilox4_32_10j",
+    "begin_iter": "_ZN3mmc10begin_iterEjPNS_5vec3fES1_fS1_P24curandStatePhilox4_32_10",
+    "calc_indexes": "_ZN3mmc12calc_indexesEjfjPjS0_PNS_5vec3fE",
+    "set_cells_empty": "_ZN3mmc15set_cells_emptyEjPjS0_",
+    "find_cells_limits": "_ZN3mmc17find_cells_limitsEjPjS0_S0_",
+    "exec_RK_1": "_ZN3mmc9exec_RK_1ILNS_5stypeE0EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_S6_"
+                 "S6_PNS_6sugridES8_",
+    "exec_RK_2": "_ZN3mmc9exec_RK_2ILNS_5stypeE0EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_S6_"
+                 "S6_S6_PNS_6sugridES8_",
+}
+
+
+def reference_gpu_step(sizes, reps=20):
+    """ccp's own per-step kernels (chrsim.cu:572-580: begin_iter, two cell-list
+    builds, exec_RK_1<DST>, exec_RK_2<DST>), compiled from the reference's
+    sources into oracle/_ref/ccp_ref.cubin, timed on this GPU with CUDA events
+    on static inputs: a relaxed configuration with ccp's force field and the
+    cell list of its positions. ccp sorts the cell keys with CUB's
+    DeviceRadixSort::SortPairs from host code, which the cubin cannot launch;
+    torch.sort(stable=True) of the same keys (CUB's radix sort as well) stands
+    in for it. Every timed launch sees the same inputs (positions are restored
+    before each exec_RK_2), so nothing can leave the cell grid. The step time
+    is the sum of the kernel times: no launch gaps, in ccp's favour."""
+    import ctypes as C
+
+    import torch
+
+    from oracle import oracle as orc
+
+    if not os.path.exists(REF_CUBIN):
+        return {"unavailable": "oracle/_ref/ccp_ref.cubin not built (needs the reference sources)"}
+    torch.cuda.init()
+    torch.zeros(1, device="cuda")
+    cu = C.CDLL("libcuda.so.1")
+
+    def ck(rc):
+        if rc != 0:
+            raise RuntimeError("CUDA driver error %d" % rc)
+
+    ck(cu.cuInit(0))
+    dev, ctx, mod = C.c_int(), C.c_void_p(), C.c_void_p()
+    ck(cu.cuDeviceGet(C.byref(dev), torch.cuda.current_device()))
+    ck(cu.cuDevicePrimaryCtxRetain(C.byref(ctx), dev))
+    ck(cu.cuCtxSetCurrent(ctx))
+    ck(cu.cuModuleLoad(C.byref(mod), REF_CUBIN.encode()))
+    fns = {}
+    for k, name in REF_NAMES.items():
+        f = C.c_void_p()
+        ck(cu.cuModuleGetFunction(C.byref(f), mod, name.encode()))
+        fns[k] = f
+    stream = torch.cuda.current_stream()
+
+    def launch(k, n, args, tpb=128):
+        ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        ck(cu.cuLaunchKernel(fns[k], max((n + tpb - 1) // tpb, 1), 1, 1, tpb, 1, 1, 0,
+                             C.c_void_p(stream.cuda_stream), ptrs, None))
+
+    class CnGeom(C.Structure):  # mmc::cngeom (chrdat.cuh:48-67), plain sphere
+        _fields_ = [(k, C.c_float) for k in ("R_n", "R_o", "R_b", "noc", "boc", "nod", "bod",
+                                             "d_b", "d_m")]
+
+    class SuGrid(C.Structure):  # mmc::sugrid (sugrid.cuh:15-32)
+        _fields_ = [("n_o", C.c_uint32), ("csl", C.c_float), ("cps", C.c_uint32),
+                    ("n_c", C.c_uint32), ("uci", C.c_uint64), ("sci", C.c_uint64),
+                    ("uoi", C.c_uint64), ("soi", C.c_uint64), ("beg", C.c_uint64),
+                    ("end", C.c_uint64), ("eb", C.c_uint64), ("ebs", C.c_uint64)]
+
+    P = lambda t: C.c_uint64(t.data_ptr())
+    dv = torch.device("cuda")
+    rco, aco = 1.154701, 2.0
+    out = []
+    rng = np.random.default_rng(11)
+    for n in sizes:
+        R = rco / 2 + rco / 2 * (n / 0.125) ** (1 / 3)  # ccp-profile.cu:55-62 (cvf 0.125)
+        n_l = int(math.floor(0.25 * 4 / ((0.5 / (R - rco)) ** 2)))
+        x = _walk(int(n), R - 0.5, rng)
+        pt = np.where(rng.random(n) < 0.5, 0, 1).astype(np.int32)
+        fl = orc.flags_from_types(pt, [0])
+        geo = orc.geo_vec(R, csl=2.0)
+        x = orc.run(x, fl, np.zeros((0, 3), np.float32), orc.ccp_ff(), geo, 1, 0, 300,
+                    mode=orc.MODE_ICG, prec=32).astype(np.float32)
+        d = rng.normal(size=(n_l, 3))
+        lbs = (d / np.linalg.norm(d, axis=1, keepdims=True) * (R - rco)).astype(np.float32)
+        ng = CnGeom(R, 0.0, 0.0, 1.0, float("nan"), R, 0.0, R, R)
+        cps = 2 * int(math.ceil(R / aco))
+        n_c = cps ** 3
+
+        def grid(pos, m):
+            t = {k: torch.zeros(max(m, 1), dtype=torch.int32, device=dv)
+                 for k in ("uci", "sci", "uoi", "soi")}
+            t["beg"] = torch.zeros(n_c, dtype=torch.int32, device=dv)
+            t["end"] = torch.zeros(n_c, dtype=torch.int32, device=dv)
+            if m:
+                launch("calc_indexes", m, [C.c_uint32(m), C.c_float(aco), C.c_uint32(cps),
+                                           P(t["uci"]), P(t["uoi"]), P(pos)])
+                keys, perm = torch.sort(t["uci"][:m], stable=True)
+                t["sci"][:m] = keys
+                t["soi"][:m] = perm.to(torch.int32)
+            launch("set_cells_empty", n_c, [C.c_uint32(n_c), P(t["beg"]), P(t["end"])])
+            if m:
+                launch("find_cells_limits", m, [C.c_uint32(m), P(t["sci"]), P(t["beg"]),
+                                                P(t["end"])])
+            g = SuGrid(m, aco, cps, n_c, *[t[k].data_ptr() for k in
+                                           ("uci", "sci", "uoi", "soi", "beg", "end")], 0, 0)
+            gd = torch.frombuffer(bytearray(bytes(g)), dtype=torch.uint8).to(dv)
+            return t, gd
+
+        r = torch.tensor(x, device=dv)
+        r0 = r.clone()
+        lr = torch.tensor(lbs if n_l else np.zeros((1, 3), np.float32), device=dv)
+        ptd = torch.tensor(pt, device=dv)
+        f, ef, er, rn = (torch.zeros((n, 3), dtype=torch.float32, device=dv) for _ in range(4))
+        ps = torch.zeros(64 * n, dtype=torch.uint8, device=dv)  # curandStatePhilox4_32_10
+        launch("init_ps", n, [C.c_uint32(n), P(ps), C.c_uint32(1)])
+        pg, pgd = grid(r, n)
+        lg, lgd = grid(lr, n_l)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+        def timed(fn, before=None):
+            fn()
+            tot = 0.0
+            for _ in range(reps):
+                if before is not None:
+                    before()
+                ev[0].record(stream)
+                fn()
+                ev[1].record(stream)
+                ev[1].synchronize()
+                tot += ev[0].elapsed_time(ev[1])
+            return tot / reps
+
+        t_begin = timed(lambda: launch("begin_iter", n, [C.c_uint32(n), P(f), P(ef),
+                                                         C.c_float(0.03125), P(rn), P(ps)]))
+        t_idx = timed(lambda: launch("calc_indexes", n, [C.c_uint32(n), C.c_float(aco),
+                                                         C.c_uint32(cps), P(pg["uci"]),
+                                                         P(pg["uoi"]), P(r)]))
+        t_sort = timed(lambda: torch.sort(pg["uci"], stable=True))
+        t_empty = timed(lambda: launch("set_cells_empty", n_c, [C.c_uint32(n_c), P(pg["beg"]),
+                                                                P(pg["end"])]))
+        t_lim = timed(lambda: launch("find_cells_limits", n, [C.c_uint32(n), P(pg["sci"]),
+                                                              P(pg["beg"]), P(pg["end"])]))
+        t_rk1 = timed(lambda: launch("exec_RK_1", n, [C.c_uint32(n), ng, P(ptd), P(r), P(f), P(lr),
+                                                      P(er), P(rn), P(pgd), P(lgd)]))
+        t_rk2 = timed(lambda: launch("exec_RK_2", n, [C.c_uint32(n), ng, P(ptd), P(r), P(f), P(lr),
+                                                      P(er), P(ef), P(rn), P(pgd), P(lgd)]),
+                      before=lambda: r.copy_(r0))
+        step = t_begin + 2 * (t_idx + t_sort + t_empty + t_lim) + t_rk1 + t_rk2
+        out.append({"n_beads": int(n), "ms_per_step": step, "bead_steps_per_s": n / (step / 1e3),
+                    "ms": {"begin_iter": t_begin, "calc_indexes": t_idx, "sort (CUB via torch)": t_sort,
+                           "set_cells_empty": t_empty, "find_cells_limits": t_lim,
+                           "exec_RK_1": t_rk1, "exec_RK_2": t_rk2}})
+        if not torch.isfinite(r).all():
+            raise RuntimeError("non-finite positions in the reference step")
+    ck(cu.cuModuleUnload(mod))
+    return {"kernels": "ccp's own sm_103a kernels (oracle/_ref/ccp_ref.cubin)",
+            "config": "ccp force field, cvf 0.125, laf 0.25 (ccp-profile.cu:55-62), cells of aco = 2",
+            "sizes": out}
+
+
 def reference_arm(args, ws, rank):
     """The reference's force/integration loop restated on the host cores (the
     reference has no CPU implementation of its loop; its kernels are
@@ -219,6 +382,11 @@ def reference_arm(args, ws, rank):
         "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if args.ref_gpu:
+        try:
+            line["reference_gpu_kernels"] = reference_gpu_step([1024, 2048, 8192, 32768])
+        except Exception as e:  # reported, not fatal: the CPU arm is the reference line
+            line["reference_gpu_kernels"] = {"unavailable": str(e)[:200]}
     print(json.dumps(line))
 
 
@@ -331,6 +499,38 @@ def engine_arm(args, ws, rank, local):
         print(json.dumps(line))
 
 
+def ccp_profile_sweep(sizes, steps=2000):
+    """The engine on ccp's own benchmark shapes (ccp-profile.cu:55-62: one
+    system, ccp force field, chromatin volume fraction 0.125, lamina area
+    fraction 0.25), ms per Heun step with CUDA events; the reference arm's
+    --ref-gpu times ccp's own kernels on the same shapes."""
+    import torch
+
+    from tfm_gb300.ccpgpu import ChrSim
+
+    rco = 1.154701
+    out = []
+    for n in sizes:
+        R = rco / 2 + rco / 2 * (n / 0.125) ** (1 / 3)
+        n_l = int(math.floor(0.25 * 4 / ((0.5 / (R - rco)) ** 2)))
+        txt = ("number_of_particles %05d\nnucleus_radius %09.6f\nnumber_of_lbs %05d\n"
+               % (n, R, n_l))
+        sim = ChrSim(txt, seed=5)
+        sim.generate_initial_condition()
+        sim.advance(200)
+        sim.synchronize()
+        st = torch.cuda.ExternalStream(sim.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.advance(steps)
+        e1.record(st)
+        sim.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out.append({"n_beads": int(n), "ms_per_step": ms, "bead_steps_per_s": n / (ms / 1e3)})
+        sim.close()
+    return out
+
+
 def measure_extras(args, sizes, b):
     """Plain engine replica by replica, the large single system, the CPU baseline."""
     import torch
@@ -376,6 +576,7 @@ def measure_extras(args, sizes, b):
         "value": 131072 * HEUN_PER_STEP * 5 / (e0.elapsed_time(e1) / 1000.0),
         "unit": "bead-steps/s", "config": "16 chains x 8192 beads, contact map 1024^2"}
     big.close()
+    out["ccp_profile"] = ccp_profile_sweep([1024, 2048, 8192, 32768])
     # CPU baseline: the FP32 oracle on the first replicas' initial conditions
     pre = []
     x = b.positions()
@@ -571,6 +772,8 @@ def main():
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
+    ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",
+                    help="reference arm: skip timing ccp's own kernels on the GPU")
     ap.add_argument("--pair-kernel", type=int, default=None,
                     help="engine pair kernel (parameter pair_kernel); default: the engine's")
     ap.add_argument("--surrogate", action="store_true",
