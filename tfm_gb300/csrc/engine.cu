@@ -56,6 +56,28 @@ struct DevBuf {
 
 constexpr int TILE = 128;
 
+// Page-locked host storage, so that copies to and from the device run as DMA
+// without a staging copy.
+template <class T>
+struct PinnedAlloc {
+  using value_type = T;
+  PinnedAlloc() = default;
+  template <class U>
+  PinnedAlloc(const PinnedAlloc<U> &) {}
+  T *allocate(size_t n) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+      throw std::bad_alloc();
+    return static_cast<T *>(p);
+  }
+  void deallocate(T *p, size_t) { cudaFreeHost(p); }
+  template <class U>
+  bool operator==(const PinnedAlloc<U> &) const { return true; }
+  template <class U>
+  bool operator!=(const PinnedAlloc<U> &) const { return false; }
+};
+using PinnedFloats = std::vector<float, PinnedAlloc<float>>;
+
 struct Engine {
   Params par;
   ForceField ff{};
@@ -72,7 +94,7 @@ struct Engine {
   int ps_total = 0;
 
   // host state
-  std::vector<float> hxyz;     // chain-order positions
+  PinnedFloats hxyz;           // chain-order positions (pinned)
   std::vector<int32_t> hpt;    // ccp type codes
   std::vector<float> hlbs;     // LBS positions, per system in placement order
   std::vector<uint32_t> hflags;
@@ -103,6 +125,7 @@ struct Engine {
   float *pinned[2] = {nullptr, nullptr};
   float4 *pin_up = nullptr;  // pinned staging of position uploads
   bool lbs_uploaded = false;
+  bool flags_current = false;  // pos.w holds the flags of the current types
   cudaStream_t stream = nullptr;
   cudaStream_t cstream = nullptr;  // device-to-host frame copies
   cudaEvent_t ev[2] = {nullptr, nullptr};       // frame copy done (cstream)
@@ -322,6 +345,22 @@ struct Engine {
     recount();
     CK(cudaStreamSynchronize(stream));
     positions_valid = true;
+    flags_current = true;
+  }
+
+  // New positions only (hxyz), the flags already on the device: one DMA of
+  // the xyz triples and a kernel that writes them under the flags.
+  void upload_xyz() {
+    if (!flags_current || !positions_valid) {
+      upload_positions();
+      return;
+    }
+    CK(cudaMemcpyAsync(xyz_stage.p, hxyz.data(), sizeof(float) * 3 * nb, cudaMemcpyHostToDevice,
+                       stream));
+    k_unpack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(xyz_stage.p, pos.p, nb);
+    CK(cudaGetLastError());
+    recount();
+    CK(cudaStreamSynchronize(stream));
   }
 
   void recount() {
@@ -652,7 +691,7 @@ struct Engine {
     if (par.pair_kernel != 2 && par.pair_kernel != 4)
       throw Error(ST_ARG, "autotune needs a half-shell pair kernel");
     download_positions();
-    std::vector<float> saved_xyz = hxyz;
+    PinnedFloats saved_xyz = hxyz;
     uint64_t saved_step = step;
     const int ns = (int)hsys.size();
     std::vector<int> cls(ns);
@@ -1006,6 +1045,7 @@ struct Engine {
         make_types_markov(d.n, par.mean_block, par.lad_fraction, rng, pt);
       std::copy(pt.begin(), pt.end(), hpt.begin() + d.bead_off);
     }
+    flags_current = false;
     upload_lbs();
     random_walk(nullptr);
     relax();
@@ -1441,7 +1481,7 @@ int ccpgpu_set_positions(ccpgpu_sim *h, const float *xyz, size_t n) {
     need(n >= (size_t)3 * e.nb, "buffer too small");
     std::memcpy(e.hxyz.data(), xyz, sizeof(float) * 3 * e.nb);
     if (!e.lbs_uploaded) e.upload_lbs();
-    e.upload_positions();
+    e.upload_xyz();
   });
 }
 
@@ -1459,6 +1499,7 @@ int ccpgpu_set_types(ccpgpu_sim *h, const int32_t *pt, size_t n) {
     Engine &e = *h->e;
     need(n >= (size_t)e.nb, "buffer too small");
     std::memcpy(e.hpt.data(), pt, 4 * (size_t)e.nb);
+    e.flags_current = false;
     if (e.positions_valid) {
       e.download_positions();
       e.upload_positions();
@@ -1568,6 +1609,7 @@ int ccpgpu_load_checkpoint(ccpgpu_sim *h, int32_t sys, const void *buf, size_t l
       throw Error(ST_IO, "failed to read checkpoint");
     if (e.positions_valid) e.download_positions();
     std::copy(pt.begin(), pt.end(), e.hpt.begin() + d.bead_off);
+    e.flags_current = false;
     std::copy(x.begin(), x.end(), e.hxyz.begin() + 3 * (size_t)d.bead_off);
     std::copy(l.begin(), l.end(), e.hlbs.begin() + 3 * (size_t)d.lbs_off);
     e.i_f[sys] = i_f;
@@ -1592,6 +1634,7 @@ int ccpgpu_read_frame_txt(ccpgpu_sim *h, int32_t sys, const char *text, size_t l
       throw Error(ST_IO, "failed to read frame from text file");
     if (e.positions_valid) e.download_positions();
     std::copy(pt.begin(), pt.end(), e.hpt.begin() + d.bead_off);
+    e.flags_current = false;
     std::copy(x.begin(), x.end(), e.hxyz.begin() + 3 * (size_t)d.bead_off);
     e.i_f[sys] = i_f;
     e.t[sys] = t;

@@ -1608,6 +1608,14 @@ k_random_walk(const WalkChain *__restrict__ chains, int n_chains, WalkParams wp,
   if (lane == 0) draws_used[c] = draw;
 }
 
+// Packed xyz triples written into the positions, keeping each bead's flags.
+__global__ void k_unpack_xyz(const float *__restrict__ xyz, float4 *__restrict__ pos, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float w = pos[i].w;
+  pos[i] = make_float4(xyz[3 * i + 0], xyz[3 * i + 1], xyz[3 * i + 2], w);
+}
+
 // Positions as packed xyz triples (the .trr / checkpoint layout).
 __global__ void k_pack_xyz(const float4 *__restrict__ pos, float *__restrict__ xyz, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
