@@ -704,7 +704,7 @@ __device__ __forceinline__ void typed_half(float4 p, uint32_t wi, int slot, Cell
 // non-A beads scan only the small stencil. RHH / RX = 0: from the system's
 // cell side (1 when it is at least the cutoff, else 2).
 template <int MODE, int RHH, int RX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
     k_pair_typed(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
                  const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                  float4 *__restrict__ fs) {
@@ -1001,7 +1001,7 @@ __device__ __forceinline__ void cap_step(float3 &D, float max_step) {
 // F = bonded + wall + LBS + pair (pair read from the cell-ordered result).
 // The written position is binned into the next counting sort.
 template <int STAGE, int MODE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 7)
     k_update(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
              float4 *__restrict__ pos, float4 *__restrict__ er, float4 *__restrict__ fbuf,
              const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
