@@ -581,7 +581,7 @@ __device__ __forceinline__ void half_range(float4 p, uint32_t wi, const float4 *
 // of 5 row ranges per bead. REACH = 0: each system's own reach (SysDesc), so
 // one launch serves systems gridded differently by the autotuner.
 template <int MODE, int REACH = 1>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
     k_pair_half(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
                 const float4 *__restrict__ sorted, const uint32_t *__restrict__ start,
                 float4 *__restrict__ fs) {
