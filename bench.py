@@ -46,7 +46,7 @@ PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4
 # DRAM bytes per bead of one pair launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) on this workload with the typed pair kernel the
 # autotuner keeps: profiles/k_pair_typed_c2.md
-PAIR_TRAFFIC_PER_BEAD = 58.3
+PAIR_TRAFFIC_PER_BEAD = 59.2
 METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
 
 
