@@ -64,7 +64,9 @@ def test_noalloc_forces_match_compute_forces(engine_lib, orc):
         torch.cuda.synchronize()
         f = d_f.cpu().numpy()
         assert np.isfinite(f).all()
-        assert _bound(f, f_alloc, sa) <= FORCE_RTOL
+        # the two paths run different pair kernels: at a truncation cutoff their
+        # FP32 distances may also fall on opposite sides
+        assert _bound(f, f_alloc, sa, skip=edge) <= FORCE_RTOL
         # beads within FP32 rounding of a jump of the truncated potential are
         # held to the jump's size (see helpers.at_cutoff)
         assert _bound(f, f64, sa, skip=edge) <= FORCE_RTOL
