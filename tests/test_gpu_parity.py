@@ -130,6 +130,32 @@ def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel, half_cells):
         assert _force_ok(fo, f64, sa) <= 1e-2
 
 
+@pytest.mark.parametrize("kernel,lanes", [(2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (4, 4)])
+def test_pair_lanes_agree(ccp_sim, base_sim, orc, kernel, lanes):
+    """The half-shell kernels (one grid, 2; typed layout, 4) with 1, 2 or 4
+    lanes per bead (rows dealt to the lanes, partial forces combined by
+    shuffles; small batches default to 4) meet the force bound, on cells of
+    half the cutoff."""
+    from tfm_gb300.ccpgpu import ChrSim
+
+    sim, R = ccp_sim
+    txt, _, _ = ccp_params(2048, laf=0.3)
+    for ref, text, ff, csl, heads in (
+            (sim, txt, orc.ccp_ff(), 2.0, [0]),
+            (base_sim, baseline_params(2048, "number_of_chains 4\n"), orc.baseline_ff(), 2.5,
+             [0, 512, 1024, 1536])):
+        other = ChrSim(text + "pair_kernel %d\npair_lanes %d\ncell_side %r\n"
+                       % (kernel, lanes, csl / 2), seed=7)
+        other.set_types(ref.types())
+        other.set_lbs(ref.lbs())
+        other.set_positions(ref.positions())
+        (f64, sa), fl, geo = _oracle_forces(orc, ref, ff, csl, heads)
+        edge = at_cutoff(ref.positions(), fl, ref.lbs(), ff)
+        fo = other.forces()
+        assert _force_ok(fo, f64, sa, skip=edge) <= FORCE_RTOL
+        assert _force_ok(fo, f64, sa) <= 1e-2
+
+
 def _golden_cases():
     return sorted(glob.glob(os.path.join(GOLDEN, "ccp_*.npz")))
 

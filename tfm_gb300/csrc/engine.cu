@@ -462,22 +462,41 @@ struct Engine {
     return key < 0 ? 0 : key;
   }
 
+  // Lanes per bead of the half-shell pair kernels: the pair_lanes parameter,
+  // or by the batch's bead count (more lanes for batches too small to fill
+  // the GPU with one thread per bead).
+  int pair_lanes() const {
+    if (par.pair_lanes > 0) return par.pair_lanes;
+    return nb < 65536 ? 4 : (nb < 262144 ? 2 : 1);
+  }
+
+  template <int MODE, int RHH, int RX>
+  void launch_typed(unsigned nt) {
+    const int L = (tile * pair_lanes() <= 512) ? pair_lanes() : 1;
+    if (L == 4)
+      k_pair_typed_lanes<MODE, RHH, RX, 4><<<nt, (unsigned)(tile * 4), 0, stream>>>(
+          d_tiles.p, d_sys.p, ff, sorted.p, start.p, fs.p);
+    else if (L == 2)
+      k_pair_typed_lanes<MODE, RHH, RX, 2><<<nt, (unsigned)(tile * 2), 0, stream>>>(
+          d_tiles.p, d_sys.p, ff, sorted.p, start.p, fs.p);
+    else
+      k_pair_typed<MODE, RHH, RX><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                           start.p, fs.p);
+  }
+
   template <int MODE>
   void launch_pair() {
     const unsigned nt = (unsigned)htiles.size();
     if (par.pair_kernel == 4) {
       switch (typed_reaches<MODE>()) {
         case 2 * 4 + 1:
-          k_pair_typed<MODE, 2, 1><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
-                                                             start.p, fs.p);
+          launch_typed<MODE, 2, 1>(nt);
           break;
         case 1 * 4 + 1:
-          k_pair_typed<MODE, 1, 1><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
-                                                             start.p, fs.p);
+          launch_typed<MODE, 1, 1>(nt);
           break;
         case 2 * 4 + 2:
-          k_pair_typed<MODE, 2, 2><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
-                                                             start.p, fs.p);
+          launch_typed<MODE, 2, 2>(nt);
           break;
         default:  // systems gridded differently: each system's own reaches
           k_pair_typed<MODE, 0, 0><<<nt, tile, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
@@ -492,7 +511,23 @@ struct Engine {
     else if (par.pair_kernel == 3)
       k_pair_flat<MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                        sorted.p, start.p, fs.p);
-    else if (par.pair_kernel == 2 && uniform_reach() == 2)
+    else if (par.pair_kernel == 2 && pair_lanes() > 1 && uniform_reach() > 0 &&
+             tile * pair_lanes() <= 512) {
+      const unsigned bs = (unsigned)(tile * pair_lanes());
+      const int r = uniform_reach();
+      if (pair_lanes() == 2 && r == 2)
+        k_pair_half_lanes<MODE, 2, 2><<<nt, bs, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+      else if (pair_lanes() == 2)
+        k_pair_half_lanes<MODE, 1, 2><<<nt, bs, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+      else if (r == 2)
+        k_pair_half_lanes<MODE, 2, 4><<<nt, bs, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+      else
+        k_pair_half_lanes<MODE, 1, 4><<<nt, bs, 0, stream>>>(d_tiles.p, d_sys.p, ff, sorted.p,
+                                                             start.p, fs.p);
+    } else if (par.pair_kernel == 2 && uniform_reach() == 2)
       k_pair_half<MODE, 2><<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, ff,
                                                                           sorted.p, start.p, fs.p);
     else if (par.pair_kernel == 2 && uniform_reach() == 1)

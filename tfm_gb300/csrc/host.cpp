@@ -214,6 +214,9 @@ Params parse_params(const std::string &text) {
   // (baseline cells of 1.25 sigma); ccp's cells of aco = 2 sigma gain nothing
   p.pair_kernel = pm.get<int>("pair_kernel", p.preset == PRESET_BASELINE ? 4 : 2);
   if (!(p.pair_kernel >= 0 && p.pair_kernel <= 4)) fail("pair_kernel out of range");
+  p.pair_lanes = pm.get<int>("pair_lanes", 0);  // 0: by the batch's bead count
+  if (!(p.pair_lanes == 0 || p.pair_lanes == 1 || p.pair_lanes == 2 || p.pair_lanes == 4))
+    fail("pair_lanes out of range");
   if (!(p.n_chains >= 1 && (uint32_t)p.n_chains <= p.N)) fail("number_of_chains out of range");
   if (!(p.contact_cutoff > 0.0f)) fail("contact_cutoff out of range");
   if (p.contact_bins < 0) fail("contact_bins out of range");

@@ -75,6 +75,7 @@ struct Params {
   // 0: full shell, thread per bead; 1: warp per cell (lane groups);
   // 2: half shell (Newton's third law), thread per bead
   int pair_kernel = 2;
+  int pair_lanes = 0;  // lanes per bead of the half-shell pair kernels (0: by bead count)
   std::string sequence_file = "Program/data/sequence.txt";
   ForceField ff{};
 };

@@ -741,6 +741,149 @@ __global__ void __launch_bounds__(256, 8)
   atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
 }
 
+// k_pair_half with L lanes per bead (blocks of tile * L threads): the bead's
+// row ranges -- its own row and the forward rows -- are dealt round-robin to
+// its L lanes, and the lanes' partial forces are combined by shuffles. For
+// systems too small to fill the GPU with one thread per bead.
+template <int MODE, int REACH, int L>
+__global__ void __launch_bounds__(512)
+    k_pair_half_lanes(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                      ForceField ff, const float4 *__restrict__ sorted,
+                      const uint32_t *__restrict__ start, float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  const int sub = threadIdx.x % L;
+  const int slot = t.begin + threadIdx.x / L;
+  const bool valid = slot < s.bead_off + s.n;
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+  float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (valid) {
+    p = sorted[slot];
+    const uint32_t wi = wbits(p);
+    bool esc = false;
+    CellXYZ c = cell_of(p, s, esc);
+    const int cps = s.cps;
+    const int x0 = max(c.x - REACH, 0), x1 = min(c.x + REACH, cps - 1);
+    const float rc_max = (MODE == MODE_ICG) ? ff.rc_icg : fmaxf(ff.rc_att, ff.rc_rep);
+    const float rc2_max = rc_max * rc_max;
+    constexpr int NR = REACH + REACH * (2 * REACH + 1);
+#pragma unroll 1
+    for (int it = sub; it <= NR; it += L) {
+      if (it == 0) {  // own cell after i, then the +x cells
+        int row = s.cell_off + (c.z * cps + c.y) * cps;
+        half_range<MODE>(p, wi, sorted, slot + 1, __ldg(&start[row + x1 + 1]), ff, rc2_max, acc,
+                         fs);
+        continue;
+      }
+      const int r = it - 1;
+      int y, z;
+      if (r < REACH) {
+        y = c.y + 1 + r;
+        z = c.z;
+      } else {
+        int q = r - REACH;
+        y = c.y - REACH + q % (2 * REACH + 1);
+        z = c.z + 1 + q / (2 * REACH + 1);
+      }
+      if (y < 0 || y >= cps || z >= cps) continue;
+      int row = s.cell_off + (z * cps + y) * cps;
+      half_range<MODE>(p, wi, sorted, __ldg(&start[row + x0]), __ldg(&start[row + x1 + 1]), ff,
+                       rc2_max, acc, fs);
+    }
+  }
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+  }
+  if (valid && sub == 0) atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
+}
+
+// Row (y, z) of forward row r of the half stencil of reach R around c (false
+// when it lies outside the grid).
+__device__ __forceinline__ bool half_row_yz(CellXYZ c, int r, int R, int cps, int &y, int &z) {
+  if (r < R) {
+    y = c.y + 1 + r;
+    z = c.z;
+  } else {
+    int q = r - R;
+    y = c.y - R + q % (2 * R + 1);
+    z = c.z + 1 + q / (2 * R + 1);
+  }
+  return y >= 0 && y < cps && z < cps;
+}
+
+// k_pair_typed with L lanes per bead (blocks of tile * L threads): the bead's
+// row ranges are numbered -- own row, forward rows of its grid, then for an A
+// bead the rows of the other grid's full stencil -- and dealt round-robin to
+// its L lanes; the lanes' partial forces are combined by shuffles.
+template <int MODE, int RHH, int RX, int L>
+__global__ void __launch_bounds__(512)
+    k_pair_typed_lanes(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
+                       ForceField ff, const float4 *__restrict__ sorted,
+                       const uint32_t *__restrict__ start, float4 *__restrict__ fs) {
+  Tile t = tiles[blockIdx.x];
+  const SysDesc &s = sys[t.sys];
+  const int sub = threadIdx.x % L;
+  const int slot = t.begin + threadIdx.x / L;
+  const bool valid = slot < s.bead_off + s.n;
+  float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+  if (valid) {
+    const float4 p = sorted[slot];
+    const uint32_t wi = wbits(p);
+    bool esc = false;
+    CellXYZ c = cell_of(p, s, esc);
+    const int cps = s.cps;
+    const float rc_hh = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_att;
+    const float rc_x = (MODE == MODE_ICG) ? ff.rc_icg : ff.rc_rep;
+    const bool isA = (wi & BF_HET) != 0u;
+    const int R = isA ? RHH : RX;
+    const int g = isA ? s.cell_off : s.cell_off + s.cls_cells;
+    const int gX = s.cell_off + s.cls_cells;
+    const int NRh = R + R * (2 * R + 1);            // forward rows of the own grid
+    const int W = 2 * RX + 1;                        // full stencil rows of the other grid
+    const int n_items = 1 + NRh + (isA ? W * W : 0);
+    const int x0 = max(c.x - R, 0), x1 = min(c.x + R, cps - 1);
+    const int xo0 = max(c.x - RX, 0), xo1 = min(c.x + RX, cps - 1);
+#pragma unroll 1
+    for (int it = sub; it < n_items; it += L) {
+      if (it == 0) {
+        int row = g + (c.z * cps + c.y) * cps;
+        if (isA)
+          typed_range<MODE, true>(p, wi, sorted, slot + 1, __ldg(&start[row + x1 + 1]), ff,
+                                  rc_hh * rc_hh, acc, fs);
+        else
+          typed_range<MODE, false>(p, wi, sorted, slot + 1, __ldg(&start[row + x1 + 1]), ff,
+                                   rc_x * rc_x, acc, fs);
+      } else if (it <= NRh) {
+        int y, z;
+        if (!half_row_yz(c, it - 1, R, cps, y, z)) continue;
+        int row = g + (z * cps + y) * cps;
+        uint32_t b = __ldg(&start[row + x0]), e = __ldg(&start[row + x1 + 1]);
+        if (isA)
+          typed_range<MODE, true>(p, wi, sorted, b, e, ff, rc_hh * rc_hh, acc, fs);
+        else
+          typed_range<MODE, false>(p, wi, sorted, b, e, ff, rc_x * rc_x, acc, fs);
+      } else {
+        const int r = it - 1 - NRh;
+        const int y = c.y + r % W - RX, z = c.z + r / W - RX;
+        if (y < 0 || y >= cps || z < 0 || z >= cps) continue;
+        int row = gX + (z * cps + y) * cps;
+        typed_range<MODE, false>(p, wi, sorted, __ldg(&start[row + xo0]),
+                                 __ldg(&start[row + xo1 + 1]), ff, rc_x * rc_x, acc, fs);
+      }
+    }
+  }
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+  }
+  if (valid && sub == 0) atomicAdd(&fs[slot], make_float4(acc.x, acc.y, acc.z, 0.0f));
+}
+
 // Half-shell pair kernel with a flattened candidate walk: each lane runs one
 // loop over its whole candidate stream and fetches the next row range only
 // when the current one is exhausted, so a warp pays the longest total stream
