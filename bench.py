@@ -479,7 +479,7 @@ def engine_arm(args, ws, rank, local):
                        "parallelism": "replicas per GPU (no collective)",
                        "autotune": None if tune is None else {
                            "pair_kernel": tune.get("pair_kernel"),
-                           "tile": tune["tile"],
+                           "tile": tune["tile"], "lanes": tune.get("lanes"),
                            "cell_side_by_class": [[c["n_min"], c["n_max"], c["cell_side"]]
                                                   for c in tune["classes"]]}},
             "clocks": clk,

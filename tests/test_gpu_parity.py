@@ -375,6 +375,7 @@ def test_autotune_keeps_state_and_forces(engine_lib, orc):
     rep = b.autotune(reps=3)
     assert len(rep["classes"]) == 3 and rep["tile"] in (64, 128, 256)
     assert rep["pair_kernel"] in (2, 4) and len(rep["kernels_tried"]) == 2
+    assert rep["lanes"] in (1, 2, 4) and rep["tile"] * rep["lanes"] <= 512
     assert np.array_equal(b.positions(), x0) and b.info().step == step0
     f = b.forces()
     pt, lbs = b.types(), b.lbs()

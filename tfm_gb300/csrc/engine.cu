@@ -660,11 +660,16 @@ struct Engine {
 
   // Rebuilds the cell grids with per-system cell sides and the per-bead tile
   // size; the state stays on the device and only the cell arrays change.
-  void regrid(const std::vector<float> &csl, int new_tile) {
+  // Drops the captured graphs (their launches depend on the kernel choice).
+  void graphs_clear() {
     CK(cudaStreamSynchronize(stream));
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
     graphs.clear();
     graph_kernels.clear();
+  }
+
+  void regrid(const std::vector<float> &csl, int new_tile) {
+    graphs_clear();
     tile = new_tile;
     nc = 0;
     for (size_t s = 0; s < hsys.size(); ++s) {
@@ -790,23 +795,30 @@ struct Engine {
         << ", " << choices[0].ms << "], [" << choices[1].kernel << ", " << choices[1].ms
         << "]], \"classes\": [" << ch.classes;
     double best = 1e30;
-    int best_tile = tile;
+    int best_tile = tile, best_lanes = pair_lanes();
     std::ostringstream tt;
     for (int t : {64, 128, 256}) {
       regrid(csl, t);
-      double ms = time_steps(reps);
-      tt << (tt.tellp() > 0 ? ", " : "") << "[" << t << ", " << ms << "]";
-      if (ms < best) {
-        best = ms;
-        best_tile = t;
+      for (int l : {1, 2, 4}) {
+        if (t * l > 512) continue;
+        par.pair_lanes = l;
+        graphs_clear();
+        double ms = time_steps(reps);
+        tt << (tt.tellp() > 0 ? ", " : "") << "[" << t << ", " << l << ", " << ms << "]";
+        if (ms < best) {
+          best = ms;
+          best_tile = t;
+          best_lanes = l;
+        }
       }
     }
+    par.pair_lanes = best_lanes;
     regrid(csl, best_tile);
     hxyz = saved_xyz;
     upload_positions();
     step = saved_step;
-    rep << "], \"tile\": " << best_tile << ", \"tiles_tried\": [" << tt.str()
-        << "], \"ms_per_step\": " << best << "}";
+    rep << "], \"tile\": " << best_tile << ", \"lanes\": " << best_lanes
+        << ", \"tiles_tried\": [" << tt.str() << "], \"ms_per_step\": " << best << "}";
     return rep.str();
   }
 
