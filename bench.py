@@ -576,6 +576,22 @@ def measure_extras(args, sizes, b):
         "value": 131072 * HEUN_PER_STEP * 5 / (e0.elapsed_time(e1) / 1000.0),
         "unit": "bead-steps/s", "config": "16 chains x 8192 beads, contact map 1024^2"}
     big.close()
+    # c0: one chain of 2048 beads, 2048^2 contact map every 100 steps
+    c0 = Batch(PARAMS.replace("contact_bins 256", "contact_bins 2048"), [2048], seeds=[1])
+    c0.generate_initial_condition()
+    c0.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    c0.synchronize()
+    st = torch.cuda.ExternalStream(c0.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(20):
+        c0.advance(HEUN_PER_STEP, HEUN_PER_STEP)
+    e1.record(st)
+    c0.synchronize()
+    out["single_system_2048"] = {
+        "value": 2048 * HEUN_PER_STEP * 20 / (e0.elapsed_time(e1) / 1000.0),
+        "unit": "bead-steps/s", "config": "c0: one chain of 2048 beads, contact map 2048^2"}
+    c0.close()
     out["ccp_profile"] = ccp_profile_sweep([1024, 2048, 8192, 32768])
     # CPU baseline: the FP32 oracle on the first replicas' initial conditions
     pre = []
