@@ -800,7 +800,7 @@ def main():
     ap.add_argument("--sur-sim-steps", type=int, default=20000)
     ap.add_argument("--sur-epochs", type=int, default=30)
     ap.add_argument("--sur-screen", type=int, default=100000)
-    ap.add_argument("--sim-rate", type=float, default=1.9e9,
+    ap.add_argument("--sim-rate", type=float, default=2.7e9,
                     help="batched bead-steps/s used to cost a simulated map (from the engine bench)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
