@@ -1335,7 +1335,7 @@ int ccpgpu_batch_create(const char *param_text, int32_t n_systems, const int32_t
     for (int s = 0; s < n_systems; ++s) {
       SystemSpec &q = sp[s];
       q.n = n_beads[s];
-      need(q.n >= 3, "system with fewer than 3 beads");
+      need(q.n >= 1, "system without beads");
       q.n_chains = n_chains ? n_chains[s] : 1;
       need(q.n_chains >= 1 && q.n_chains <= q.n, "bad chain count");
       if (radii)
