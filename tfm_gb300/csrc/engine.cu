@@ -545,8 +545,8 @@ struct Engine {
   template <int STAGE, int MODE>
   void launch_update() {
     k_update<STAGE, MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(
-        d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, start.p, counts.p,
-        lbs_sorted.p, lbs_start.p, d_step.p, d_err.p);
+        d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, counts.p, lbs_sorted.p,
+        lbs_start.p, d_step.p, d_err.p);
     kcount += 1;
   }
 
@@ -1065,7 +1065,7 @@ struct Engine {
     sort_now();
     launch_pair<MODE_DST>();
     k_total_force<MODE_DST><<<(unsigned)htiles.size(), tile, 0, stream>>>(
-        d_tiles.p, d_sys.p, ff, pos.p, fs.p, rank.p, start.p, lbs_sorted.p, lbs_start.p, fout.p);
+        d_tiles.p, d_sys.p, ff, pos.p, fs.p, rank.p, lbs_sorted.p, lbs_start.p, fout.p);
     recount();
     CK(cudaGetLastError());
     k_pack_xyz<<<(nb + 255) / 256, 256, 0, stream>>>(fout.p, xyz_stage.p, nb);
@@ -1992,8 +1992,8 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
     k_scan_apply<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum, start, nc, nblk);
     k_scatter<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, rank, start, sorted, fs, err);
     k_pair_half<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, sorted, start, fs);
-    k_total_force<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, pos, fs, rank, start,
-                                                     nullptr, nullptr, fout);
+    k_total_force<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, pos, fs, rank, nullptr,
+                                                     nullptr, fout);
     k_pack_xyz<<<(a.n_beads + 255) / 256, 256, 0, s>>>(fout, d_forces, a.n_beads);
     CK(cudaGetLastError());
   });

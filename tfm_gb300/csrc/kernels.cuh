@@ -401,9 +401,11 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 // ------------------------------------------------------------------ scatter
 
 // Counting-sort scatter: bead i goes to slot start[cell] + rank[i] of the
-// cell-ordered copy, with its global index packed above the flag bits.
+// cell-ordered copy, with its global index packed above the flag bits; the
+// slot replaces the rank in rank[i], so the passes that read the pair force
+// back in chain order (update, total force) need no cell lookup.
 __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
-                          const float4 *__restrict__ src, const uint32_t *__restrict__ rank,
+                          const float4 *__restrict__ src, uint32_t *__restrict__ rank,
                           const uint32_t *__restrict__ start, float4 *__restrict__ sorted,
                           float4 *__restrict__ fs_clear, int *__restrict__ err) {
   Tile t = tiles[blockIdx.x];
@@ -422,6 +424,7 @@ __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restr
   }
   uint32_t w = ((uint32_t)i << BF_BITS) | (wbits(p) & 7u);
   sorted[slot] = make_float4(p.x, p.y, p.z, __uint_as_float(w));
+  rank[i] = slot;
 }
 
 // ------------------------------------------------------------------ pair
@@ -1148,7 +1151,7 @@ __global__ void __launch_bounds__(256, 7)
     k_update(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
              float4 *__restrict__ pos, float4 *__restrict__ er, float4 *__restrict__ fbuf,
              const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
-             const uint32_t *__restrict__ start, uint32_t *__restrict__ counts,
+             uint32_t *__restrict__ counts,
              const float4 *__restrict__ lbs, const uint32_t *__restrict__ lbs_start,
              const unsigned long long *__restrict__ step, int *__restrict__ err) {
   Tile t = tiles[blockIdx.x];
@@ -1160,10 +1163,9 @@ __global__ void __launch_bounds__(256, 7)
   float4 xi = X[i];
   uint32_t fl = wbits(xi);
 
-  // pair force of this bead from the cell-ordered pass
-  bool esc = false;
-  int c_old = bead_cell(xi, s, esc);
-  uint32_t slot = start[c_old] + rank[i];
+  // pair force of this bead from the cell-ordered pass (its slot, left in
+  // rank[i] by the scatter)
+  uint32_t slot = rank[i];
   float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end)
     fp = fs[slot];
@@ -1228,7 +1230,7 @@ template <int MODE>
 __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
                               ForceField ff, const float4 *__restrict__ pos,
                               const float4 *__restrict__ fs, const uint32_t *__restrict__ rank,
-                              const uint32_t *__restrict__ start, const float4 *__restrict__ lbs,
+                              const float4 *__restrict__ lbs,
                               const uint32_t *__restrict__ lbs_start, float4 *__restrict__ out) {
   Tile t = tiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
@@ -1236,9 +1238,7 @@ __global__ void k_total_force(const Tile *__restrict__ tiles, const SysDesc *__r
   int end = s.bead_off + s.n;
   if (i >= end) return;
   float4 xi = pos[i];
-  bool esc = false;
-  int c = bead_cell(xi, s, esc);
-  uint32_t slot = start[c] + rank[i];
+  uint32_t slot = rank[i];  // left by the scatter
   float4 fp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (slot >= (uint32_t)s.bead_off && slot < (uint32_t)end) fp = fs[slot];
   float3 F = make_float3(fp.x, fp.y, fp.z);
