@@ -18,6 +18,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -55,6 +56,29 @@ struct DevBuf {
 };
 
 constexpr int TILE = 128;
+
+// Host copy of a large position array split over a few threads: one thread
+// copies well below the host's memory bandwidth, and the end-to-end path
+// copies the positions in and out every step.
+static void host_copy(void *dst, const void *src, size_t bytes) {
+  const size_t min_chunk = size_t(4) << 20;
+  unsigned nt = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  nt = (unsigned)std::min<size_t>(nt, std::max<size_t>(1, bytes / min_chunk));
+  if (nt <= 1) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t chunk = (bytes + nt - 1) / nt;
+  for (unsigned k = 0; k < nt; ++k) {
+    size_t b = k * chunk, e = std::min(bytes, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([=] {
+      std::memcpy(static_cast<char *>(dst) + b, static_cast<const char *>(src) + b, e - b);
+    });
+  }
+  for (auto &t : th) t.join();
+}
 
 // Page-locked host storage, so that copies to and from the device run as DMA
 // without a staging copy.
@@ -1517,7 +1541,7 @@ int ccpgpu_get_positions(ccpgpu_sim *h, float *xyz, size_t n) {
     Engine &e = *h->e;
     need(n >= (size_t)3 * e.nb, "buffer too small");
     if (e.positions_valid) e.download_positions();
-    std::memcpy(xyz, e.hxyz.data(), sizeof(float) * 3 * e.nb);
+    host_copy(xyz, e.hxyz.data(), sizeof(float) * 3 * e.nb);
   });
 }
 
@@ -1526,7 +1550,7 @@ int ccpgpu_set_positions(ccpgpu_sim *h, const float *xyz, size_t n) {
     need(h && xyz, "null argument");
     Engine &e = *h->e;
     need(n >= (size_t)3 * e.nb, "buffer too small");
-    std::memcpy(e.hxyz.data(), xyz, sizeof(float) * 3 * e.nb);
+    host_copy(e.hxyz.data(), xyz, sizeof(float) * 3 * e.nb);
     if (!e.lbs_uploaded) e.upload_lbs();
     e.upload_xyz();
   });
