@@ -4,8 +4,8 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
 legs import this module; the engine never does. The constants below restate
 the reference's model constants independently of the engine's code:
   ccp preset      Program/src/chrdat.cuh:15-24, chrsim.cuh:18-20, chrsim.cu:424
-  baseline preset the BASELINE configs (harmonic k=100, cosine kappa=2, WCA +
-                  A-A LJ eps=0.5 to 2.5 sigma, WCA wall, kT=1, dt=1e-3)
+  baseline preset the benchmark force field (harmonic k=100, cosine kappa=2,
+                  WCA + A-A LJ eps=0.5 to 2.5 sigma, WCA wall, kT=1, dt=1e-3)
 """
 import ctypes as C
 import math
