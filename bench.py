@@ -463,7 +463,7 @@ def engine_arm(args, ws, rank, local):
         extras = measure_extras(args, sizes, b)
         b.close()
         extras["surrogate"] = surrogate_report(value / ws, n_seq=1024, sim_steps=10000, epochs=30,
-                                               judge_reps=3, screen_n=0)
+                                               truth_reps=3, screen_n=0)
 
     if rank == 0:
         line = {
@@ -627,11 +627,11 @@ def bf16_peak():
         return 1900.0, "fallback"
 
 
-def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, judge_reps, screen_n, seed=7):
+def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, truth_reps, screen_n, seed=7):
     """Simulate contact maps of n_seq seeded sequences (1024 beads, 256 bins)
     with the batched engine, train the surrogate on 90 % of them with its own
     tensor-core kernels, score the held-out 10 % (P(s) error per separation
-    octave against the simulation, against the mean of `judge_reps` fresh
+    octave against the simulation, against the mean of `truth_reps` fresh
     replica simulations, and the same numbers for a second simulation and for
     the training set's mean map), time batched inference with the inputs on
     the device and through the C ABI with host buffers, and optionally screen
@@ -650,8 +650,8 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, judge_reps, scr
     held = np.arange(ntr, n_seq, dtype=np.int32)
     k = min(64, nh)
     reps = [S.simulate_maps(types[ntr:ntr + k], lad[ntr:ntr + k], SUR_M, sim_steps, burn, every,
-                            seed=1000 + 17 * r)[0] for r in range(judge_reps)]
-    judge = np.mean(reps, axis=0)
+                            seed=1000 + 17 * r)[0] for r in range(truth_reps)]
+    truth = np.mean(reps, axis=0)
     mean_map = maps[:ntr].mean(axis=0, keepdims=True)
     B = 32
     steps_total = epochs * max(1, ntr // B)
@@ -669,21 +669,21 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, judge_reps, scr
         "simulate_s": t_sim, "train_s": t_train, "epochs": epochs, "optimizer_steps": steps_total,
         "heldout_loss": hist[-1].get("heldout_loss"),
         "ps_error": {"vs_simulation": float(e.mean()),
-                     "vs_mean_of_%d_replicas" % judge_reps: float(S.ps_error(pred[:k], judge).mean()),
+                     "vs_mean_of_%d_replicas" % truth_reps: float(S.ps_error(pred[:k], truth).mean()),
                      "metric": "mean over separation octaves [1,2)..[64,128) of |P_pred - P_sim| / P_sim"},
         "baselines": {
             "second_simulation_vs_simulation": float(S.ps_error(reps[0], maps[ntr:ntr + k]).mean()),
             "second_simulation_vs_mean_of_others": float(S.ps_error(
-                reps[0], np.mean(reps[1:], axis=0)).mean()) if judge_reps > 2 else None,
+                reps[0], np.mean(reps[1:], axis=0)).mean()) if truth_reps > 2 else None,
             "training_mean_map_vs_simulation": float(S.ps_error(np.repeat(mean_map, nh, 0), maps[ntr:]).mean()),
-            "training_mean_map_vs_mean_of_replicas": float(S.ps_error(np.repeat(mean_map, k, 0), judge).mean()),
+            "training_mean_map_vs_mean_of_replicas": float(S.ps_error(np.repeat(mean_map, k, 0), truth).mean()),
         },
         # per bin pair, against the replica mean (one run is mostly zero counts far
         # from the diagonal, which an expected-probability predictor cannot match)
         "map_log10_mae_vs_mean_of_replicas": {
-            "surrogate": float(S.map_log_error(pred[:k], judge).mean()),
-            "one_simulation": float(S.map_log_error(maps[ntr:ntr + k], judge).mean()),
-            "training_mean_map": float(S.map_log_error(np.repeat(mean_map, k, 0), judge).mean())},
+            "surrogate": float(S.map_log_error(pred[:k], truth).mean()),
+            "one_simulation": float(S.map_log_error(maps[ntr:ntr + k], truth).mean()),
+            "training_mean_map": float(S.map_log_error(np.repeat(mean_map, k, 0), truth).mean())},
     }
     # inference throughput, inputs resident: batches of dataset rows
     st = torch.cuda.ExternalStream(net.stream())

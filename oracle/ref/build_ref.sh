@@ -2,7 +2,7 @@
 # Compiles the reference's device code (Program/src/chrsim.cu, sugrid.cu,
 # chrana.cu, read where they lie under the reference checkout) into
 # oracle/_ref/ccp_ref.cubin for sm_103a. Device code only: the cubin is loaded
-# on the GPU machine through the CUDA driver API by tests/golden/make_golden.py.
+# on a GB300 through the CUDA driver API by tests/golden/make_golden.py.
 # Usage: oracle/ref/build_ref.sh [reference_root]   (default /root/reference)
 set -e
 REF=${1:-/root/reference}

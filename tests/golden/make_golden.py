@@ -13,7 +13,8 @@ set of seeded inputs, runs:
 and stores inputs and outputs in <out_dir>/<case>.npz. Inputs are seeded
 synthetic configurations (no reference data files are read).
 
-Usage (on a GPU machine):  python tests/golden/make_golden.py [out_dir]
+Usage (on a machine with a GB300):  python tests/golden/make_golden.py [out_dir]
+(out_dir defaults to tests/golden, the fixtures' own folder)
 """
 import ctypes as C
 import math
@@ -280,7 +281,7 @@ def near_cutoff_pairs(rng, n_pairs):
 
 
 def main():
-    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden")
+    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden")
     os.makedirs(out_dir, exist_ok=True)
     cuda = Cuda()
     rng = np.random.default_rng(20261203)

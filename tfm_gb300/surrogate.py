@@ -361,7 +361,7 @@ def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
     """Batched inference over many sequences with a simulation fallback: a
     random `fallback_fraction` of them, plus every sequence whose predicted
     P(s) leaves the envelope in some separation octave, is re-simulated by
-    `sim` (a callable (types, lad) -> maps), which judges the prediction.
+    `sim` (a callable (types, lad) -> maps), whose maps check the prediction.
     Returns a report and the indices re-simulated."""
     import time
 
