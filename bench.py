@@ -401,8 +401,19 @@ def engine_arm(args, ws, rank, local):
     from tfm_gb300.ccpgpu import Batch
 
     torch.cuda.set_device(local)
-    sizes = replica_sizes(args.replicas)
-    seeds = replicas.replica_seeds(args.replicas, rank)  # disjoint per rank
+    if args.split:
+        # one fixed ensemble split over the ranks by bead count (strong scaling);
+        # every replica keeps its seed, so the ensemble does not depend on N
+        if args.replicas < ws:
+            raise SystemExit("--split needs at least one replica per rank")
+        ensemble = replica_sizes(args.replicas)
+        _, sizes, seeds = replicas.local_replicas(
+            ensemble, np.arange(args.replicas, dtype=np.uint64) + 1, ws, rank)
+        job_beads = int(ensemble.sum())
+    else:
+        sizes = replica_sizes(args.replicas)
+        seeds = replicas.replica_seeds(args.replicas, rank)  # disjoint per rank
+        job_beads = ws * int(sizes.sum())  # weak scaling: N ensembles
     params = PARAMS + ("pair_kernel %d\n" % args.pair_kernel if args.pair_kernel is not None else "")
     b = Batch(params, sizes, seeds=seeds)
     b.generate_initial_condition()
@@ -435,7 +446,7 @@ def engine_arm(args, ws, rank, local):
     ms = ev0.elapsed_time(ev1)
     launches = b.kernel_count() - k0
     ms = max_over_ranks(ms, ws)
-    value = replicas.whole_job_rate(total * HEUN_PER_STEP * args.steps, ws, ms / 1000.0)
+    value = job_beads * HEUN_PER_STEP * args.steps / (ms / 1000.0)  # all ranks' beads / slowest
     ms_step = ms / args.steps
 
     # dominant kernel (pair) timed live with CUDA events on the engine stream
@@ -456,7 +467,7 @@ def engine_arm(args, ws, rank, local):
         x = b.positions()  # D2H of the step's result
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, ws)
-    e2e_val = replicas.whole_job_rate(total * HEUN_PER_STEP * args.steps, ws, e2e_s)
+    e2e_val = job_beads * HEUN_PER_STEP * args.steps / e2e_s
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -469,14 +480,16 @@ def engine_arm(args, ws, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
+            "higher_is_better": True, "scaling": "strong" if args.split else "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": "c2: %d replicas, N_i log-uniform [1024, 16384], baseline "
                                    "force field, 256^2 int32 contact maps every 100 steps"
                                    % args.replicas,
-                       "total_beads": total, "heun_steps_per_step": HEUN_PER_STEP,
+                       "total_beads": total, "job_beads": job_beads,
+                       "heun_steps_per_step": HEUN_PER_STEP,
                        "l2": "state (~%d MB) larger than the 129 MB L2" % (total * 100 // 2**20),
-                       "parallelism": "replicas per GPU (no collective)",
+                       "parallelism": ("one ensemble split over GPUs by bead count" if args.split
+                                       else "replicas per GPU (no collective)"),
                        "autotune": None if tune is None else {
                            "pair_kernel": tune.get("pair_kernel"),
                            "tile": tune["tile"], "lanes": tune.get("lanes"),
@@ -787,6 +800,9 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--split", action="store_true",
+                    help="split one ensemble of --replicas over the GPUs (strong scaling) "
+                         "instead of one ensemble per GPU")
     ap.add_argument("--no-tune", action="store_true", help="skip the per-class autotuner")
     ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",
                     help="reference arm: skip timing ccp's own kernels on the GPU")

@@ -361,6 +361,41 @@ def test_batch_matches_single_systems(engine_lib):
         off += n
 
 
+def test_ensemble_split_matches_whole_batch(engine_lib):
+    """A fixed ensemble split over two ranks by bead count (each rank's share
+    a batch of its own, replicas keeping their seeds) reproduces the whole
+    batch: same types and lamina sites, and after 200 steps from the same
+    start the same positions to FP32 summation order."""
+    from tfm_gb300 import replicas
+    from tfm_gb300.ccpgpu import Batch
+
+    txt = "force_field baseline\ncontact_bins 64\n"
+    sizes = np.array([1024, 3000, 1536, 2048, 1100], dtype=np.int32)
+    seeds = np.arange(len(sizes), dtype=np.uint64) + 21
+    b = Batch(txt, sizes, seeds=seeds)
+    b.generate_initial_condition()
+    x0, pt, lbs = b.positions(), b.types(), b.lbs()
+    b.run_steps(200)
+    xb = b.positions()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for rank in range(2):
+        idx, sz, sd = replicas.local_replicas(sizes, seeds, 2, rank)
+        part = Batch(txt, sz, seeds=sd)
+        part.generate_initial_condition()
+        rows = np.concatenate([np.arange(off[k], off[k + 1]) for k in idx])
+        assert np.array_equal(part.types(), pt[rows])
+        for j, k in enumerate(idx):
+            si, sj = b.system_info(int(k)), part.system_info(j)
+            assert np.array_equal(part.lbs()[sj.lbs_offset:sj.lbs_offset + sj.n_lbs],
+                                  lbs[si.lbs_offset:si.lbs_offset + si.n_lbs])
+        part.set_positions(x0[rows])
+        part.run_steps(200)
+        d = np.abs(part.positions() - xb[rows]).max()
+        assert d < 1e-3, (rank, d)
+        part.close()
+    b.close()
+
+
 def test_autotune_keeps_state_and_forces(engine_lib, orc):
     """The autotuner picks a pair kernel, re-grids size classes and picks a
     tile size without changing positions or time, and forces stay within the

@@ -5,6 +5,9 @@ maximum of the ranks' timings (the whole job is as slow as its slowest rank).
 
 Each rank draws its replicas' seeds from its own disjoint range, so an N-rank
 job simulates N distinct ensembles (weak scaling: the work per GPU is fixed).
+A fixed ensemble is instead split over the ranks by bead count
+(split_replicas / local_replicas: strong scaling), each replica keeping its
+seed.
 """
 import os
 
@@ -49,6 +52,37 @@ def replica_seeds(n_replicas, rank):
     if not 0 < n_replicas < SEED_STRIDE:
         raise ValueError("replicas per rank must be in [1, %d)" % SEED_STRIDE)
     return np.arange(n_replicas, dtype=np.uint64) + 1 + SEED_STRIDE * rank
+
+
+def split_replicas(sizes, ws):
+    """Partition of a fixed ensemble over ws ranks, balanced by bead count:
+    replicas in decreasing size (ties by index) each go to the rank with the
+    fewest beads so far (ties to the lowest rank), the longest-processing-
+    time-first rule, whose largest load is at most 4/3 of the optimum. Returns
+    one sorted index array per rank. Every rank computes the same partition
+    from the same sizes, so no collective is needed."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if ws < 1:
+        raise ValueError("world size must be at least 1")
+    if sizes.ndim != 1 or (sizes < 1).any():
+        raise ValueError("replica sizes must be a list of positive bead counts")
+    order = sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k))
+    load = [0] * ws
+    parts = [[] for _ in range(ws)]
+    for k in order:
+        r = min(range(ws), key=lambda q: (load[q], q))
+        parts[r].append(k)
+        load[r] += int(sizes[k])
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
+
+
+def local_replicas(sizes, seeds, ws, rank):
+    """This rank's share of a fixed ensemble (strong scaling): the global
+    indices from split_replicas and their sizes and seeds. A replica keeps its
+    global seed, so its trajectory does not depend on the number of ranks."""
+    idx = split_replicas(sizes, ws)[rank]
+    return (idx, np.asarray(sizes, dtype=np.int32)[idx],
+            np.asarray(seeds, dtype=np.uint64)[idx])
 
 
 def barrier(ws):
