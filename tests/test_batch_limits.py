@@ -1,0 +1,27 @@
+"""Batch sizes the engine cannot address are refused at creation, before any
+device memory is touched (so these run without a GPU): the sorted words
+carry a bead's batch index in 29 bits, one system's grid has at most 1024
+cells per side, and cells are addressed with 32-bit ints."""
+import pytest
+
+from tfm_gb300.ccpgpu import Batch, CcpError
+
+PARAMS = "force_field baseline\n"
+
+
+def test_too_many_beads():
+    with pytest.raises(CcpError, match="more than 536870911 beads"):
+        Batch(PARAMS, [1 << 28, 1 << 28])
+
+
+def test_grid_side_limit():
+    # 10 beads in a nucleus of radius 700: 1120 cells of 1.25 sigma per side
+    with pytest.raises(CcpError, match="more than 1024 cells per side"):
+        Batch(PARAMS, [10], radii=[700.0])
+
+
+def test_total_cells_limit():
+    # three grids of 800^3 cells each, twice over in the typed layout
+    with pytest.raises(CcpError, match="cells; use a larger cell_side"):
+        Batch(PARAMS, [10, 10, 10], radii=[500.0, 500.0, 500.0])
+

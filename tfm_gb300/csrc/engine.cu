@@ -56,6 +56,9 @@ struct DevBuf {
 };
 
 constexpr int TILE = 128;
+constexpr int MAX_CPS = 1024;  // cells per side of one system's grid
+constexpr uint32_t MAX_BATCH_BEADS = (1u << (32u - BF_BITS)) - 1u;
+constexpr int64_t MAX_BATCH_CELLS = (int64_t)INT32_MAX - 4 * (int64_t)SCAN_CHUNK;
 
 // Host copy of a large position array split over a few threads: one thread
 // copies well below the host's memory bandwidth, and the end-to-end path
@@ -176,6 +179,9 @@ struct Engine {
     ff = p.ff;
     specs = std::move(sp);
     int ns = (int)specs.size();
+    int64_t beads = 0;
+    for (const auto &q : specs) beads += q.n;
+    check_totals(beads, 0);
     hsys.resize(ns);
     geo.resize(ns);
     i_f.assign(ns, 0);
@@ -198,8 +204,8 @@ struct Engine {
       d.n = q.n;
       d.csl = p.cell_side;
       d.inv_csl = 1.0f / p.cell_side;
-      d.cps = 2 * (int)std::ceil(g.d_m / p.cell_side);
-      if (d.cps < 2) d.cps = 2;
+      d.cps = grid_side(g.d_m, p.cell_side);
+      check_totals(beads, (int64_t)nc + cells_of(d.cps));
       d.cell_off = nc;
       d.cls_cells = typed() ? d.cps * d.cps * d.cps : 0;
       d.R_n = g.R_n;
@@ -254,7 +260,7 @@ struct Engine {
       map_total += (int64_t)d.nbins * (d.nbins + 1) / 2;
       hsys[s] = d;
       nb += q.n;
-      nc += (typed() ? 2 : 1) * d.cps * d.cps * d.cps;
+      nc += (int)cells_of(d.cps);
       nl += q.n_lbs;
     }
     need_cut = std::max({ff.rc_att, ff.rc_rep, ff.rc_icg, p.contact_cutoff, ff.mis});
@@ -470,6 +476,29 @@ struct Engine {
   // Typed layout (pair_kernel 4): A beads and the others sorted into separate
   // cell grids of each system.
   bool typed() const { return par.pair_kernel == 4; }
+
+  // Cells per side of a system's grid: the cube of side 2 d_m (d_m = the
+  // largest distance of a bead from the centre) in cells of side csl.
+  static int grid_side(float d_m, float csl) {
+    float half = std::ceil(d_m / csl);
+    if (!(half <= (float)(MAX_CPS / 2)))
+      throw Error(ST_ARG, "nucleus too large for the cell side (more than " +
+                              std::to_string(MAX_CPS) + " cells per side)");
+    return std::max(2, 2 * (int)half);
+  }
+
+  // Cells of one system: one grid, or two in the typed layout.
+  int64_t cells_of(int cps) const { return (typed() ? 2 : 1) * (int64_t)cps * cps * cps; }
+
+  // The sorted words carry a bead's batch index in 32 - BF_BITS bits, and
+  // cells are addressed with 32-bit ints (plus the scan's padding).
+  static void check_totals(int64_t beads, int64_t cells) {
+    if (beads > (int64_t)MAX_BATCH_BEADS)
+      throw Error(ST_ARG, "batch holds more than " + std::to_string(MAX_BATCH_BEADS) + " beads");
+    if (cells > MAX_BATCH_CELLS)
+      throw Error(ST_ARG, "batch needs more than " + std::to_string(MAX_BATCH_CELLS) +
+                              " cells; use a larger cell_side or fewer systems");
+  }
 
   // Stencil reaches of the typed pair kernel for MODE when every system has
   // the same (A-A reach * 4 + other reach), else 0.
@@ -693,6 +722,9 @@ struct Engine {
   }
 
   void regrid(const std::vector<float> &csl, int new_tile) {
+    int64_t total = 0;
+    for (size_t s = 0; s < hsys.size(); ++s) total += cells_of(grid_side(geo[s].d_m, csl[s]));
+    check_totals(nb, total);
     graphs_clear();
     tile = new_tile;
     nc = 0;
@@ -700,11 +732,11 @@ struct Engine {
       SysDesc &d = hsys[s];
       d.csl = csl[s];
       d.inv_csl = 1.0f / csl[s];
-      d.cps = std::max(2, 2 * (int)std::ceil(geo[s].d_m / csl[s]));
+      d.cps = grid_side(geo[s].d_m, csl[s]);
       d.cell_off = nc;
       d.reach = (csl[s] >= need_cut) ? 1 : 2;
       d.cls_cells = typed() ? d.cps * d.cps * d.cps : 0;
-      nc += (typed() ? 2 : 1) * d.cps * d.cps * d.cps;
+      nc += (int)cells_of(d.cps);
     }
     build_tiles();
     nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
