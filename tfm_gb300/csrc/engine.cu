@@ -3,6 +3,8 @@
 // Memory layout in HBM (all systems concatenated, chain order):
 //   pos, er          float4 per bead: x, y, z, flags (BF_*) in w
 //   fbuf             float4 per bead: stage-1 force (f of chrsim.cu:387)
+//   rnb              float4 per bead: the step's noise, drawn by stage 1 and
+//                    reused by stage 2 (one rn per step, chrsim.cu:387, :415)
 //   sorted           float4 per bead in cell order: x, y, z, (index << 3 | flags)
 //   fs               float4 per bead in cell order: pair force
 //   rank             uint32 per bead: rank of the bead inside its cell
@@ -136,7 +138,7 @@ struct Engine {
   // device state
   DevBuf<SysDesc> d_sys;
   DevBuf<Tile> d_tiles, d_ctiles;
-  DevBuf<float4> pos, er, fbuf, fs, sorted, lbs_sorted, fout;
+  DevBuf<float4> pos, er, fbuf, rnb, fs, sorted, lbs_sorted, fout;
   DevBuf<uint32_t> rank, counts, start, bsum, lbs_start;
   DevBuf<int32_t> d_chain_of, d_chain_first, d_chain_len, d_chain_ps_off, d_chain_smax;
   DevBuf<int32_t> map, ps;
@@ -285,6 +287,7 @@ struct Engine {
     pos.alloc(nb + 1);
     er.alloc(nb + 1);
     fbuf.alloc(nb + 1);
+    rnb.alloc(nb + 1);
     fs.alloc(nb + 1);
     sorted.alloc(nb + 1);
     fout.alloc(nb + 1);
@@ -330,6 +333,7 @@ struct Engine {
     CK(cudaMemsetAsync(pos.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(er.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(fbuf.p, 0, sizeof(float4) * (nb + 1), stream));
+    CK(cudaMemsetAsync(rnb.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(fs.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(sorted.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(lbs_start.p, 0, sizeof(uint32_t) * (nc + 1), stream));
@@ -598,7 +602,7 @@ struct Engine {
   template <int STAGE, int MODE>
   void launch_update() {
     k_update<STAGE, MODE><<<(unsigned)htiles.size(), tile, 0, stream>>>(
-        d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, fs.p, rank.p, counts.p, lbs_sorted.p,
+        d_tiles.p, d_sys.p, ff, pos.p, er.p, fbuf.p, rnb.p, fs.p, rank.p, counts.p, lbs_sorted.p,
         lbs_start.p, d_step.p, d_err.p);
     kcount += 1;
   }

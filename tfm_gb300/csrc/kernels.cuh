@@ -1145,12 +1145,13 @@ __device__ __forceinline__ void cap_step(float3 &D, float max_step) {
 //   STAGE 1: X = r.  f = F(r);  er = r + f dt + sd z           (chrsim.cu:365-388)
 //   STAGE 2: X = er. ef = F(er); r = r + (f + ef) dt / 2 + sd z (chrsim.cu:392-416)
 // F = bonded + wall + LBS + pair (pair read from the cell-ordered result).
+// Stage 1 draws the step's noise sd z and keeps it in rnb for stage 2.
 // The written position is binned into the next counting sort.
 template <int STAGE, int MODE>
 __global__ void __launch_bounds__(256, 7)
     k_update(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys, ForceField ff,
              float4 *__restrict__ pos, float4 *__restrict__ er, float4 *__restrict__ fbuf,
-             const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
+             float4 *__restrict__ rnb, const float4 *__restrict__ fs, uint32_t *__restrict__ rank,
              uint32_t *__restrict__ counts,
              const float4 *__restrict__ lbs, const uint32_t *__restrict__ lbs_start,
              const unsigned long long *__restrict__ step, int *__restrict__ err) {
@@ -1195,8 +1196,14 @@ __global__ void __launch_bounds__(256, 7)
 
   float3 rn = make_float3(0.0f, 0.0f, 0.0f);
   if (MODE == MODE_DST && ff.sd > 0.0f) {
-    float3 z = bead_noise((uint32_t)(i - s.bead_off), *step, s.seed_lo, s.seed_hi, err);
-    rn = make_float3(ff.sd * z.x, ff.sd * z.y, ff.sd * z.z);
+    if (STAGE == 1) {
+      float3 z = bead_noise((uint32_t)(i - s.bead_off), *step, s.seed_lo, s.seed_hi, err);
+      rn = make_float3(ff.sd * z.x, ff.sd * z.y, ff.sd * z.z);
+      rnb[i] = make_float4(rn.x, rn.y, rn.z, 0.0f);
+    } else {
+      float4 r4 = rnb[i];
+      rn = make_float3(r4.x, r4.y, r4.z);
+    }
   }
 
   float4 out;
