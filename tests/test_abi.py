@@ -43,6 +43,19 @@ def test_library_exports_every_declared_symbol(engine_lib):
     ("force_field lj\n", "force_field out of range"),
     ("force_field baseline\nnumber_of_particles 1000\ncell_side 1.0\n",
      "cell_side below interaction cutoff"),
+    ("force_field baseline\nnumber_of_particles 1000\npair_kernel 7\n", "pair_kernel out of range"),
+    ("force_field baseline\nnumber_of_particles 1000\npair_lanes 3\n", "pair_lanes out of range"),
+    ("force_field baseline\nnumber_of_particles 1000\nnumber_of_chains 1001\n",
+     "number_of_chains out of range"),
+    ("force_field baseline\nnumber_of_particles 1000\ncontact_cutoff 0\n",
+     "contact_cutoff out of range"),
+    ("force_field baseline\nnumber_of_particles 1000\nlad_fraction 1.5\n",
+     "lad_fraction out of range"),
+    ("force_field baseline\nnumber_of_particles 1000\nmean_block_length 0.5\n",
+     "mean_block_length out of range"),
+    # kernels 0 and 1 need cells of the full cutoff (no 5x5x5 stencil)
+    ("force_field baseline\nnumber_of_particles 1000\npair_kernel 0\ncell_side 1.25\n",
+     "cell_side below interaction cutoff"),
 ])
 def test_parameter_errors_use_ccp_messages(engine_lib, text, msg):
     from tfm_gb300 import ccpgpu
