@@ -441,6 +441,12 @@ class Batch(_Handle):
         nc = None if n_chains is None else np.ascontiguousarray(n_chains, np.int32)
         rd = None if radii is None else np.ascontiguousarray(radii, np.float32)
         sd = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
+        # the C side reads one entry per system from each array
+        if nb.ndim != 1 or ns == 0:
+            raise ValueError("n_beads must be a non-empty list of bead counts")
+        for name, a in (("n_chains", nc), ("radii", rd), ("seeds", sd)):
+            if a is not None and a.shape != (ns,):
+                raise ValueError("%s must have one entry per system (%d)" % (name, ns))
         self._keep = (nb, nc, rd, sd)
         _check(_lib.ccpgpu_batch_create(
             param_text.encode(), ns, _ptr(nb), None if nc is None else _ptr(nc),
