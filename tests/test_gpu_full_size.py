@@ -66,6 +66,10 @@ def test_c1_system_forces(engine_lib, orc):
     above = int((e[~edge] > FORCE_RTOL).sum())
     print("c1 forces: bound %.3g, %d beads above %g (%d of %d beads at a cutoff)"
           % (inner, above, FORCE_RTOL, edge.sum(), n))
+    worst = np.flatnonzero(~edge)[np.argsort(e[~edge])[-3:]]
+    for i in worst:  # the tail beads: error, |F_64| and the sum of term magnitudes S
+        print("  bead %d: ratio %.3g  |dF| %.3g  |F| %.4g  S %.4g" % (
+            i, e[i], np.linalg.norm(fg[i] - f64[i]), np.linalg.norm(f64[i]), sa[i]))
     # FP32 tail at this size: the bound holds for all but a few of the 131072
     # beads, and the rare bead above it stays within twice the bound
     assert above <= n // 10000 and inner <= 2 * FORCE_RTOL and every <= 1e-2
