@@ -1041,6 +1041,7 @@ __device__ __forceinline__ float3 lbs_force(float4 x, const SysDesc &s, const Fo
   int yl = cell_coord(x.y - m, s.inv_csl, s.cps, esc), yh = cell_coord(x.y + m, s.inv_csl, s.cps, esc);
   int zl = cell_coord(x.z - m, s.inv_csl, s.cps, esc), zh = cell_coord(x.z + m, s.inv_csl, s.cps, esc);
   const float cl = ff.e_l * (8.0f / (3.0f * ff.lco * ff.lco));
+  const float l2h = __fmul_rn(ff.lco, ff.lco), l2l = __fmaf_rn(ff.lco, ff.lco, -l2h);
   for (int z = zl; z <= zh; ++z)
     for (int y = yl; y <= yh; ++y) {
       int row = s.cell_off + (z * s.cps + y) * s.cps;
@@ -1048,11 +1049,13 @@ __device__ __forceinline__ float3 lbs_force(float4 x, const SysDesc &s, const Fo
       for (uint32_t k = b; k < e; ++k) {
         float4 q = lbs[k];
         float vx = x.x - q.x, vy = x.y - q.y, vz = x.z - q.z;
-        float dl = sqrtf(vx * vx + vy * vy + vz * vz);
-        if (dl > ff.lco) continue;
-        float nd = dl / ff.lco;
-        float n2 = nd * nd;
-        float cf = cl * (n2 * n2 * n2 - 1.0f);
+        // (d/lco)^6 - 1 = (n2 - 1)(n2^2 + n2 + 1) with n2 - 1 = (d^2 - lco^2) / lco^2:
+        // no cancellation as d -> lco, where the force goes to zero
+        float dd = sq3_minus(vx, vy, vz, l2h, l2l);
+        if (dd > 0.0f) continue;  // beyond the cutoff
+        float m1 = dd / l2h;
+        float n2 = 1.0f + m1;
+        float cf = cl * m1 * (n2 * n2 + n2 + 1.0f);
         f.x += cf * vx;
         f.y += cf * vy;
         f.z += cf * vz;
