@@ -104,7 +104,9 @@ __host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b,
 // Philox4x32 with 10 rounds (Salmon, Moraes, Dror, Shaw; SC'11).
 __host__ __device__ __forceinline__ U32x4 philox4x32_10(U32x4 c, uint32_t k0,
                                                         uint32_t k1) {
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     uint32_t hi0, lo0, hi1, lo1;
     mulhilo32(0xD2511F53u, c.x, hi0, lo0);
