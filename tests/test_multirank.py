@@ -115,3 +115,14 @@ def test_split_replicas_balance_and_cover():
             replicas.split_replicas(bad, 2)
     with pytest.raises(ValueError):
         replicas.split_replicas([1, 2], 0)
+
+
+def test_local_replicas_checks_its_arguments():
+    from tfm_gb300 import replicas
+
+    with pytest.raises(ValueError, match="one seed per replica"):
+        replicas.local_replicas([10, 20, 30], [1, 2], 2, 0)
+    with pytest.raises(ValueError, match="outside a world"):
+        replicas.local_replicas([10, 20], [1, 2], 2, 2)
+    idx, sz, sd = replicas.local_replicas([10, 20, 30], [7, 8, 9], 2, 1)
+    assert idx.tolist() == [0, 1] and sz.tolist() == [10, 20] and sd.tolist() == [7, 8]

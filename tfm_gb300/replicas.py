@@ -80,9 +80,14 @@ def local_replicas(sizes, seeds, ws, rank):
     """This rank's share of a fixed ensemble (strong scaling): the global
     indices from split_replicas and their sizes and seeds. A replica keeps its
     global seed, so its trajectory does not depend on the number of ranks."""
+    if not 0 <= rank < ws:
+        raise ValueError("rank %d outside a world of %d" % (rank, ws))
+    sizes = np.asarray(sizes)
+    seeds = np.asarray(seeds, dtype=np.uint64)
+    if seeds.shape != sizes.shape:
+        raise ValueError("one seed per replica is needed")
     idx = split_replicas(sizes, ws)[rank]
-    return (idx, np.asarray(sizes, dtype=np.int32)[idx],
-            np.asarray(seeds, dtype=np.uint64)[idx])
+    return idx, sizes.astype(np.int32)[idx], seeds[idx]
 
 
 def barrier(ws):
