@@ -81,8 +81,9 @@ static inline REAL SFX(sq3_minus)(REAL a, REAL b, REAL c, REAL kh, REAL kl) {
   return s3 + (((ea + eb) + (ec + e1)) + ((e2 + e3) - kl));
 }
 
-/* Pair force coefficient c, F_i += c (r_i - r_j) (chrsim.cu:174-198). */
-static inline REAL SFX(pair_c)(REAL d, int hh, const SFX(model) * m, int mode) {
+/* Pair force coefficient c, F_i += c (r_i - r_j) (chrsim.cu:174-198), for the
+ * pair vector v of length d. */
+static inline REAL SFX(pair_c)(SFX(v3) v, REAL d, int hh, const SFX(model) * m, int mode) {
   if (mode == MODE_ICG) {
     if (d > m->rc_icg) return 0;
     return m->k_icg * (3 * m->rc_icg - 3 * d);
@@ -103,6 +104,16 @@ static inline REAL SFX(pair_c)(REAL d, int hh, const SFX(model) * m, int mode) {
   REAL e = hh ? m->e_att : m->e_rep;
   REAL i2 = 1 / (d * d), i6 = i2 * i2 * i2;
 #if ORC_ACCURATE
+  /* the repulsive class near its cutoff 2^(1/6), the force's zero:
+   * 2 d^-6 - 1 = -(d^2 - 2^(1/3)) (d^4 + 2^(1/3) d^2 + 2^(2/3)) d^-6 from an
+   * error-free d^2 - 2^(1/3) (the engine's lj_coef) */
+  if (!hh) {
+    const REAL z2h = (REAL)1.259921074e+00, z2l = (REAL)-2.401870169e-08;
+    REAL d2 = d * d;
+    REAL t = SFX(sq3_minus)(v.x, v.y, v.z, z2h, z2l);
+    REAL q = fma(d2, d2 + z2h, (REAL)1.587401032e+00);
+    return 24 * e * (i6 * i2) * (-t * q * i6);
+  }
   return 24 * e * (i6 * i2) * fma((REAL)2, i6, (REAL)-1);
 #else
   return 24 * e * (2 * i6 * i6 - i6) * i2;
@@ -331,7 +342,7 @@ static void SFX(forces_core)(int n, const SFX(v3) * r, const uint32_t *flags, in
               if (abs(i - j) <= 1) continue;
               SFX(v3) v = SFX(sub)(ri, r[j]);
               REAL d = SQRT(SFX(dot)(v, v));
-              REAL c2 = SFX(pair_c)(d, ai && (flags[j] & F_A), m, mode);
+              REAL c2 = SFX(pair_c)(v, d, ai && (flags[j] & F_A), m, mode);
               f.x += c2 * v.x; f.y += c2 * v.y; f.z += c2 * v.z;
               sa += fabs(c2) * d;
             }
@@ -341,7 +352,7 @@ static void SFX(forces_core)(int n, const SFX(v3) * r, const uint32_t *flags, in
         if (abs(i - j) <= 1) continue;
         SFX(v3) v = SFX(sub)(ri, r[j]);
         REAL d = SQRT(SFX(dot)(v, v));
-        REAL c2 = SFX(pair_c)(d, ai && (flags[j] & F_A), m, mode);
+        REAL c2 = SFX(pair_c)(v, d, ai && (flags[j] & F_A), m, mode);
         f.x += c2 * v.x; f.y += c2 * v.y; f.z += c2 * v.z;
         sa += fabs(c2) * d;
       }

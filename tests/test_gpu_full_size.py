@@ -3,9 +3,7 @@ that do not grow with the system beyond what the oracle does in seconds:
 
   * one 131072-bead system (16 chains of 8192, baseline force field): every
     bead's force against the FP64 oracle after 200 steps (cell-list oracle,
-    O(N)); the 1e-5 bound holds for all but at most 1 in 10^4 beads, and
-    every bead within 2e-5 (the largest of ~1e5 FP32 force sums reaches
-    7e-6 - 1.2e-5 from run to run);
+    O(N)) within the 1e-5 bound;
   * the 512-replica ensemble (2.79 M beads, log-uniform sizes 1024-16384):
     after the initial condition and 200 steps no device flag is set (no
     non-finite position, no bead outside its grid, no counting-sort slot
@@ -70,9 +68,7 @@ def test_c1_system_forces(engine_lib, orc):
     for i in worst:  # the tail beads: error, |F_64| and the sum of term magnitudes S
         print("  bead %d: ratio %.3g  |dF| %.3g  |F| %.4g  S %.4g" % (
             i, e[i], np.linalg.norm(fg[i] - f64[i]), np.linalg.norm(f64[i]), sa[i]))
-    # FP32 tail at this size: the bound holds for all but a few of the 131072
-    # beads, and the rare bead above it stays within twice the bound
-    assert above <= n // 10000 and inner <= 2 * FORCE_RTOL and every <= 1e-2
+    assert above == 0 and inner <= FORCE_RTOL and every <= 1e-2
     b.close()
 
 

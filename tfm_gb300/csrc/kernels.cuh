@@ -124,15 +124,57 @@ __device__ __forceinline__ float wf_coef(float e, float d2) {
   return 6.0f * e * (__fsub_rn(d2, 4.0f) * __fmaf_rn(3.0f, d2, -4.0f)) * (i4 * i4);
 }
 
-// Lennard-Jones coefficient 24 e (2 / d^14 - 1 / d^8) = 24 e d^-8 (2 d^-6 - 1).
-__device__ __forceinline__ float lj_coef(float e, float d2) {
-  float i2 = 1.0f / d2, i6 = i2 * i2 * i2;
-  return 24.0f * e * (i6 * i2) * __fmaf_rn(2.0f, i6, -1.0f);
+// 2^(1/3), the squared distance of the Lennard-Jones force's zero (the WCA
+// cutoff 2^(1/6)), as a pair of FP32 words, and its square.
+constexpr float LJ_Z2_HI = 1.259921074e+00f;
+constexpr float LJ_Z2_LO = -2.401870169e-08f;
+constexpr float LJ_Z2_SQ = 1.587401032e+00f;
+
+// d^2 - 2^(1/3) for the pair vector (dx, dy, dz), |components| < 2, without
+// cancellation: each component is split as x = xh + xl with xh on a 2^-10
+// grid (rounded by adding and subtracting 1.5 * 2^13), so xh^2 and the sum of
+// the three are exact in FP32 and the sum minus 2^(1/3) is exact (Sterbenz)
+// for d^2 within a factor 2 of it; x^2 - xh^2 = xl (xh + x) is small.
+__device__ __forceinline__ float lj_zero_gap(float dx, float dy, float dz) {
+  const float M = 12288.0f;
+  float xh = __fsub_rn(__fadd_rn(dx, M), M), yh = __fsub_rn(__fadd_rn(dy, M), M),
+        zh = __fsub_rn(__fadd_rn(dz, M), M);
+  float sh = __fmaf_rn(zh, zh, __fmaf_rn(yh, yh, __fmul_rn(xh, xh)));
+  float lo = __fmaf_rn(__fsub_rn(dx, xh), __fadd_rn(xh, dx),
+                       __fmaf_rn(__fsub_rn(dy, yh), __fadd_rn(yh, dy),
+                                 __fmaf_rn(__fsub_rn(dz, zh), __fadd_rn(zh, dz), -LJ_Z2_LO)));
+  return __fadd_rn(__fsub_rn(sh, LJ_Z2_HI), lo);
 }
 
-// Coefficient c of a pair force F_i = c (r_i - r_j) (chrsim.cu:174-198).
+// Lennard-Jones coefficient 24 e (2 / d^14 - 1 / d^8) = 24 e d^-8 (2 d^-6 - 1)
+// for the pair vector (dx, dy, dz) with FP32 squared length d2. The factor
+// 2 d^-6 - 1 cancels at the force's zero, the WCA cutoff of the repulsive
+// class: from a rounded d2 it carries an absolute error of ~5e-7, up to
+// 3e-6 kT/sigma on the pair force there. For that class (ZERO_GAP) it is
+// formed as
+//   2 d^-6 - 1 = -(d^2 - 2^(1/3)) (d^4 + 2^(1/3) d^2 + 2^(2/3)) d^-6
+// from the error-free d^2 - 2^(1/3) above, so its error stays relative to
+// itself. The attractive A-A class (half the well depth, cut at 2.5 sigma)
+// keeps the plain form: its pairs near the zero are measured not to set the
+// force error.
+template <bool ZERO_GAP>
+__device__ __forceinline__ float lj_coef(float e, float dx, float dy, float dz, float d2) {
+  float i2 = 1.0f / d2, i6 = i2 * i2 * i2;
+  float m;
+  if (ZERO_GAP) {
+    float q = __fmaf_rn(d2, __fadd_rn(d2, LJ_Z2_HI), LJ_Z2_SQ);
+    m = -lj_zero_gap(dx, dy, dz) * q * i6;
+  } else {
+    m = __fmaf_rn(2.0f, i6, -1.0f);
+  }
+  return 24.0f * e * (i6 * i2) * m;
+}
+
+// Coefficient c of a pair force F_i = c (r_i - r_j) (chrsim.cu:174-198) for
+// the pair vector (dx, dy, dz) of squared length d2.
 template <int MODE>
-__device__ __forceinline__ float pair_coef(float d2, bool hh, const ForceField &ff) {
+__device__ __forceinline__ float pair_coef(float dx, float dy, float dz, float d2, bool hh,
+                                           const ForceField &ff) {
   if (MODE == MODE_ICG) {
     // soft repulsion 128 (3 rco - 3 d) (chrsim.cu:189-198)
     if (d2 > ff.rc_icg * ff.rc_icg) return 0.0f;
@@ -142,7 +184,7 @@ __device__ __forceinline__ float pair_coef(float d2, bool hh, const ForceField &
   float rc = hh ? ff.rc_att : ff.rc_rep;
   if (d2 > rc * rc) return 0.0f;
   if (ff.pot == POT_WF) return wf_coef(ff.e_att, d2);
-  return lj_coef(hh ? ff.e_att : ff.e_rep, d2);
+  return hh ? lj_coef<false>(ff.e_att, dx, dy, dz, d2) : lj_coef<true>(ff.e_rep, dx, dy, dz, d2);
 }
 
 // Distance d of (a, b, c) from the origin and the gap g = R - d carried as a
@@ -429,9 +471,10 @@ __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restr
 
 // ------------------------------------------------------------------ pair
 
-// Branch-free pair term of the pair kernels: the coefficient is
-// evaluated for every candidate and selected to zero beyond the cutoff or for
-// |i - j| <= 1 (self included), so the lanes of a warp never diverge. The
+// Pair term of the warp-per-cell kernel: the coefficient is evaluated for
+// every candidate and selected to zero beyond the cutoff or for |i - j| <= 1
+// (self included), so the lanes of a warp diverge only between the two
+// Lennard-Jones classes (lj_coef). The
 // reciprocal is the hardware approximation (<= 2 ulp), well inside the FP32
 // force tolerance.
 template <int MODE>
@@ -450,14 +493,11 @@ __device__ __forceinline__ void pair_accum(float4 p, uint32_t wi, float4 q, cons
   } else {
     bool hh = (wi & wj & BF_HET) != 0u;
     float rc = hh ? ff.rc_att : ff.rc_rep;
-    float i2 = __fdividef(1.0f, d2);
     if (ff.pot == POT_WF) {
-      float i4 = i2 * i2;
+      float i2 = __fdividef(1.0f, d2), i4 = i2 * i2;
       cf = 6.0f * ff.e_att * (__fsub_rn(d2, 4.0f) * __fmaf_rn(3.0f, d2, -4.0f)) * (i4 * i4);
     } else {
-      float e = hh ? ff.e_att : ff.e_rep;
-      float i6 = i2 * i2 * i2;
-      cf = 24.0f * e * (i6 * i2) * __fmaf_rn(2.0f, i6, -1.0f);
+      cf = hh ? lj_coef<false>(ff.e_att, dx, dy, dz, d2) : lj_coef<true>(ff.e_rep, dx, dy, dz, d2);
     }
     cf = (excl || d2 > rc * rc) ? 0.0f : cf;
   }
@@ -501,7 +541,7 @@ __global__ void __launch_bounds__(256)
         bool hh = (wi & wj & BF_HET) != 0u;
         float rc = (MODE == MODE_ICG) ? ff.rc_icg : (hh ? ff.rc_att : ff.rc_rep);
         if (d2 > rc * rc || (unsigned)(gi - gj + 1) <= 2u) continue;
-        float cf = pair_coef<MODE>(d2, hh, ff);
+        float cf = pair_coef<MODE>(dx, dy, dz, d2, hh, ff);
         acc.x += cf * dx;
         acc.y += cf * dy;
         acc.z += cf * dz;
@@ -530,7 +570,7 @@ __device__ __forceinline__ void half_pair(float4 p, uint32_t wi, const float4 *_
   bool hh = (wi & wj & BF_HET) != 0u;
   float rc = (MODE == MODE_ICG) ? ff.rc_icg : (hh ? ff.rc_att : ff.rc_rep);
   if (d2 > rc * rc || (unsigned)(gi - gj + 1) <= 2u) return;
-  float cf = pair_coef<MODE>(d2, hh, ff);
+  float cf = pair_coef<MODE>(dx, dy, dz, d2, hh, ff);
   float fx = cf * dx, fy = cf * dy, fz = cf * dz;
   acc.x += fx;
   acc.y += fy;
@@ -556,7 +596,7 @@ __device__ __forceinline__ void half_pair_q(float4 p, uint32_t wi, float4 q, uin
   }
   int gi = (int)(wi >> BF_BITS), gj = (int)(wj >> BF_BITS);
   if ((unsigned)(gi - gj + 1) <= 2u) return;
-  float cf = pair_coef<MODE>(d2, hh, ff);
+  float cf = pair_coef<MODE>(dx, dy, dz, d2, hh, ff);
   float fx = cf * dx, fy = cf * dy, fz = cf * dz;
   acc.x += fx;
   acc.y += fy;
@@ -640,7 +680,7 @@ __device__ __forceinline__ void typed_pair(float4 p, uint32_t wi, float4 q, uint
   if (d2 > rc2) return;
   int gi = (int)(wi >> BF_BITS), gj = (int)(wbits(q) >> BF_BITS);
   if ((unsigned)(gi - gj + 1) <= 2u) return;
-  float cf = pair_coef<MODE>(d2, HH, ff);
+  float cf = pair_coef<MODE>(dx, dy, dz, d2, HH, ff);
   float fx = cf * dx, fy = cf * dy, fz = cf * dz;
   acc.x += fx;
   acc.y += fy;
