@@ -2,9 +2,12 @@
 # Builds oracle/_ref/sostat_driver (host code only, no GPU needed) from the
 # reference's statistics and utilities (Program/src/sostat.cu, util.cu, read
 # where they lie under the reference checkout) and oracle/ref/sostat_driver.cu.
-# Usage: oracle/ref/build_sostat.sh [reference_root]   (default /root/reference)
+# Usage: oracle/ref/build_sostat.sh [reference_root]
+#   reference_root: argument, else $CCP_REFERENCE_ROOT, else /root/reference;
+#   exits 3 when no checkout is there (build() then keeps the prebuilt files)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${CCP_REFERENCE_ROOT:-/root/reference}}
+[ -d "$REF/Program/src" ] || { echo "no reference checkout at $REF" >&2; exit 3; }
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"
 mkdir -p "$OUT"
