@@ -284,7 +284,10 @@ int ccpgpu_contact_map_bin(ccpgpu_sim *h, char *buf, size_t cap, size_t *len);
  * CCPGPU_NOALLOC_MAX_BEADS and cells_per_side^3 <= CCPGPU_NOALLOC_MAX_CELLS;
  * larger systems are rejected with CCPGPU_ERR_ARG. The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture on that device. Every call uses the same array and
+ * before any stream capture on that device; the address is kept for the
+ * process, so it is not valid after cudaDeviceReset on that device. The call
+ * reports argument errors only: read the device flags of a call with
+ * ccpgpu_noalloc_error_flags. Every call uses the same array and
  * it keeps the last call's contents: calls that overlap on the GPU (on
  * different streams without ordering) race and corrupt each other. */
 #define CCPGPU_NOALLOC_MAX_BEADS 32768
@@ -293,12 +296,22 @@ int ccpgpu_contact_map_bin(ccpgpu_sim *h, char *buf, size_t cap, size_t *len);
 typedef struct ccpgpu_noalloc_system {
   int32_t preset;       /* 0 = ccp, 1 = baseline */
   int32_t n_beads;      /* 3 .. CCPGPU_NOALLOC_MAX_BEADS */
-  int32_t n_chains;     /* equal chains */
-  float nucleus_radius; /* spherical nucleus */
+  int32_t n_chains;     /* heads at c * (n_beads / n_chains); the last chain takes the rest */
+  float nucleus_radius; /* spherical nucleus, finite and > 1 */
 } ccpgpu_noalloc_system;
 
 int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sys, const float *d_xyz,
                           const int32_t *d_types, float *d_forces, void *stream);
+
+/* The eight device flags (the layout of ccpgpu_error_flags) of the last
+ * ccpgpu_forces_noalloc call on the current device; allocates nothing. Pass
+ * the stream of that call: the copy is ordered after it and the function
+ * waits for it. Returns CCPGPU_ERR_STATE when a position was not finite or a
+ * cell slot inconsistent; flags8[1] reports a bead outside the nucleus's cell
+ * grid (clamped to the border cell). Like the forces call, it shares the
+ * static array, so a call overlapping another on the GPU reads its flags.
+ * No counterpart in the reference (ccp throws from cuda_check, util.cu:83-91). */
+int ccpgpu_noalloc_error_flags(int32_t *flags8, void *stream);
 
 #ifdef __cplusplus
 }

@@ -32,7 +32,8 @@ SYMBOLS = (
     "ccpgpu_reset_observables", "ccpgpu_contact_counts", "ccpgpu_observable_sums",
     "ccpgpu_separation_counts", "ccpgpu_overlaps", "ccpgpu_advance", "ccpgpu_synchronize",
     "ccpgpu_stream_handle", "ccpgpu_kernel_times", "ccpgpu_kernel_count",
-    "ccpgpu_forces_noalloc", "ccpgpu_autotune", "ccpgpu_analysis_frame", "ccpgpu_analysis_series",
+    "ccpgpu_forces_noalloc", "ccpgpu_noalloc_error_flags", "ccpgpu_autotune",
+    "ccpgpu_analysis_frame", "ccpgpu_analysis_series",
     "ccpgpu_analysis_end_simulation", "ccpgpu_analysis_txt", "ccpgpu_analysis_fin_txt",
     "ccpgpu_contact_map_bin", "ccpgpu_random_walk",
 )
@@ -119,6 +120,7 @@ def load(path=LIB_PATH):
         "ccpgpu_kernel_times": [P, I32, P, SZ],
         "ccpgpu_kernel_count": [P, C.POINTER(C.c_uint64)],
         "ccpgpu_forces_noalloc": [C.POINTER(NoallocSystem), P, P, P, P],
+        "ccpgpu_noalloc_error_flags": [P, P],
         "ccpgpu_autotune": [P, I32, P, SZ, C.POINTER(SZ)],
         "ccpgpu_analysis_frame": [P], "ccpgpu_analysis_end_simulation": [P],
         "ccpgpu_analysis_series": [P, I32, P, SZ, C.POINTER(I32)],
@@ -416,6 +418,15 @@ def forces_noalloc(preset, n_beads, n_chains, nucleus_radius, d_xyz, d_types, d_
     s = NoallocSystem(int(preset), int(n_beads), int(n_chains), float(nucleus_radius))
     return _lib.ccpgpu_forces_noalloc(C.byref(s), C.c_void_p(d_xyz), C.c_void_p(d_types),
                                       C.c_void_p(d_forces), C.c_void_p(stream or None))
+
+
+def noalloc_error_flags(stream=0):
+    """(status, flags[8]) of the last forces_noalloc call on the current device,
+    after the given stream has run it."""
+    load()
+    a = np.zeros(8, np.int32)
+    rc = _lib.ccpgpu_noalloc_error_flags(_ptr(a), C.c_void_p(stream or None))
+    return rc, a
 
 
 def last_error():

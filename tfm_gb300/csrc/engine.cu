@@ -1957,9 +1957,11 @@ __global__ void k_na_setup(SysDesc d, Tile *tiles, SysDesc *sys, int n_tiles) {
 }
 
 // Packed xyz + ccp type codes -> float4 positions with the bead flags of the
-// preset; chain heads every L beads (equal chains).
+// preset; n_chains chain heads at c * L, L = n / n_chains, the last chain
+// taking the remainder (as the allocating engine places them).
 __global__ void k_na_pack(const float *__restrict__ xyz, const int32_t *__restrict__ pt, int n,
-                          int chain_len, int preset, float4 *__restrict__ pos) {
+                          int chain_len, int n_chains, int preset, float4 *__restrict__ pos,
+                          int *__restrict__ err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > n) return;
   uint32_t f = BF_START;
@@ -1969,10 +1971,11 @@ __global__ void k_na_pack(const float *__restrict__ xyz, const int32_t *__restri
     bool a = (pt[i] & 1) == 0;
     if (a) f |= BF_HET;
     if (preset == PRESET_CCP ? a : ((pt[i] & 2) != 0)) f |= BF_LAD;
-    if (i % chain_len == 0) f |= BF_START;
+    if (i % chain_len == 0 && i / chain_len < n_chains) f |= BF_START;
     x = xyz[3 * i];
     y = xyz[3 * i + 1];
     z = xyz[3 * i + 2];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) set_err(err, ERR_NAN);
   }
   pos[i] = make_float4(x, y, z, __uint_as_float(f));
 }
@@ -1991,7 +1994,8 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
       throw Error(ST_ARG, "n_beads outside 3.." + std::to_string(MAX_BEADS) +
                               " (the no-allocation scratch limit)");
     need(a.n_chains >= 1 && a.n_chains <= a.n_beads, "bad chain count");
-    need(a.nucleus_radius > 1.0f, "nucleus radius too small");
+    need(std::isfinite(a.nucleus_radius) && a.nucleus_radius > 1.0f,
+         "nucleus radius not finite or too small");
     // the preset force field and cell grid (as parse_params sets them)
     ForceField ff = make_preset(a.preset);
     const float csl = (a.preset == PRESET_CCP) ? CCP_ACO : std::max(ff.rc_att, 1.5f);
@@ -2001,7 +2005,13 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
     d.n = a.n_beads;
     d.csl = csl;
     d.inv_csl = 1.0f / csl;
-    d.cps = std::max(2, 2 * (int)std::ceil(g.d_m / csl));
+    // bound the half side in float before it becomes an int: the grid of the
+    // largest allowed nucleus is far below this, so only the cell limit applies
+    const float half = std::ceil(g.d_m / csl);
+    if (!(half <= 64.0f))
+      throw Error(ST_ARG, "cell grid exceeds the " + std::to_string(MAX_CELLS) +
+                              "-cell no-allocation limit");
+    d.cps = std::max(2, 2 * (int)half);
     long long cells = (long long)d.cps * d.cps * d.cps;
     if (cells > MAX_CELLS)
       throw Error(ST_ARG, "cell grid of " + std::to_string(cells) + " cells exceeds the " +
@@ -2045,7 +2055,7 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
     CK(cudaMemsetAsync(err, 0, sizeof(int) * ERR_COUNT, s));
     k_na_setup<<<(n_tiles + 127) / 128, 128, 0, s>>>(d, tiles, sys, n_tiles);
     k_na_pack<<<(a.n_beads + 1 + 255) / 256, 256, 0, s>>>(
-        d_xyz, d_types, a.n_beads, std::max(1, a.n_beads / a.n_chains), a.preset, pos);
+        d_xyz, d_types, a.n_beads, a.n_beads / a.n_chains, a.n_chains, a.preset, pos, err);
     k_count<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, counts, rank, err);
     k_scan_reduce<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum);
     k_scan_top<<<1, SCAN_TOP_THREADS, 0, s>>>(bsum, nblk, step, 0);
@@ -2056,5 +2066,25 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
                                                      nullptr, fout);
     k_pack_xyz<<<(a.n_beads + 255) / 256, 256, 0, s>>>(fout, d_forces, a.n_beads);
     CK(cudaGetLastError());
+  });
+}
+
+// Device flags of the last ccpgpu_forces_noalloc call on the current device,
+// read after the caller's stream has finished that call. Non-finite positions
+// and inconsistent cell slots are reported as CCPGPU_ERR_STATE, as
+// ccpgpu_error_flags does for a handle; an escaped bead (clamped into the
+// border cell of the grid) only sets its flag.
+extern "C" int ccpgpu_noalloc_error_flags(int32_t *flags8, void *stream) {
+  using namespace ccpgpu::noalloc;
+  return guarded([&] {
+    need(flags8 != nullptr, "null argument");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    need(dev >= 0 && dev < MAX_DEVICES, "device index out of range");
+    const int *err = reinterpret_cast<const int *>(scratch_base(dev) + OFF_ERR);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(flags8, err, sizeof(int) * ERR_COUNT, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (flags8[ERR_NAN] || flags8[ERR_SLOT]) throw Error(ST_STATE, "device error flag set");
   });
 }
