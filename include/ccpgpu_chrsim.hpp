@@ -1,17 +1,22 @@
 // Header-only drop-in for ccp's simulation class over the C ABI of libccpgpu.
 //
-// Replaces the class mmc::chrsim of Program/src/chrsim.cuh:36-100 (and the
-// frame I/O it inherits from mmc::chrdat, chrdat.cuh:81-100) with the same
-// public member functions, so ccp-perform.cu (Program/src/ccp-perform.cu:48-111)
-// and ccp-profile.cu (:74-82) compile unchanged. It relies on the caller's own
-// mmc::parmap, mmc::error and mmc::logger (Program/src/util.cuh:20-80), which
-// must be declared before this header is included; streams are filled from the
-// byte images the library returns.
+// Replaces Program/src/chrsim.cuh: the class mmc::chrsim (chrsim.cuh:36-100,
+// and the frame I/O it inherits from mmc::chrdat, chrdat.cuh:81-100) with the
+// same public member functions, and the constants dt and mis
+// (chrsim.cuh:18-20) that ccp's programs read, so ccp-perform.cu
+// (Program/src/ccp-perform.cu:48-111) and ccp-profile.cu (:55-86) compile
+// unchanged. It relies on the caller's own mmc::parmap, mmc::error and
+// mmc::logger (Program/src/util.cuh:20-80) and, in ccp, on chrdat.cuh for the
+// model constants (rco, lco): a maintainer replaces the body of chrsim.cuh with
+//   #include "chrdat.cuh"
+//   #include "ccpgpu_chrsim.hpp"
+// Streams are filled from the byte images the library returns.
 #ifndef CCPGPU_CHRSIM_HPP
 #define CCPGPU_CHRSIM_HPP
 
 #include <cstdint>
 #include <cstring>
+#include <ctime>
 #include <fstream>
 #include <iterator>
 #include <sstream>
@@ -22,14 +27,22 @@
 
 namespace mmc {
 
+// ccp's timestep and minimum initial separation (chrsim.cuh:18-20);
+// ccp-profile.cu:82 turns frames into steps with dt. The engine's ccp preset
+// uses the same values.
+static constexpr float dt = 1.0 / 2048;
+static constexpr float mis = 0.838732;
+
 class chrsim {
  public:
   // chrsim::chrsim(parmap&) (chrsim.cu:421-455): the parameter map is handed
-  // to the engine as the text of adjustable-parameters.dat.
+  // to the engine as the text of adjustable-parameters.dat. Like ccp
+  // (chrsim.cu:454), the noise is seeded with the time unless the file has a
+  // "seed" key.
   explicit chrsim(parmap &par) {
     std::string text;
     for (const auto &kv : par) text += kv.first + " " + kv.second + "\n";
-    check(ccpgpu_create(text.c_str(), 0, &h_));
+    check(ccpgpu_create(text.c_str(), (uint64_t)std::time(nullptr), &h_));
   }
   ~chrsim() { ccpgpu_destroy(h_); }
   chrsim(const chrsim &) = delete;
