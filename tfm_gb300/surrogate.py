@@ -270,10 +270,16 @@ def counts_to_probability(tri, bins, frames, beads_per_bin):
     return (m / (frames * pairs)).astype(np.float32)
 
 
-def simulate_maps(types, lad, bins, steps, burn_in, every, seed, params=ENGINE_PARAMS):
-    """Contact-probability maps [n][bins][bins] of one engine replica per
-    sequence, simulated together in one batch. Returns (maps, frames)."""
+def simulate_maps(types, lad, bins, steps, burn_in, every, seed, params=ENGINE_PARAMS, reps=1):
+    """Contact-probability maps [n][bins][bins] of the sequences, simulated
+    together in one batch: with reps > 1 each sequence is run by `reps`
+    replicas (their own seeds and initial conditions) and its map is their
+    mean. Returns (maps, frames)."""
     types = np.asarray(types)
+    if reps > 1:
+        maps, frames = simulate_maps(np.repeat(types, reps, 0), np.repeat(np.asarray(lad), reps, 0),
+                                     bins, steps, burn_in, every, seed, params)
+        return maps.reshape(types.shape[0], reps, bins, bins).mean(axis=1), frames
     n, L = types.shape
     text = params + "contact_bins %d\nsteps_per_frame %d\n" % (bins, every)
     seeds = np.arange(n, dtype=np.uint64) + np.uint64(seed)
@@ -292,21 +298,39 @@ def simulate_maps(types, lad, bins, steps, burn_in, every, seed, params=ENGINE_P
     return maps, frames
 
 
-def ps_curve(maps):
-    """P(s) for s = 0 .. bins - 1: mean of each diagonal band, per map."""
-    maps = np.asarray(maps, np.float64)
+def ps_curve(maps, smax=None):
+    """P(s) for s = 0 .. smax - 1 (default bins - 1): mean of each diagonal
+    band, per map."""
+    maps = np.asarray(maps)
     n, M, _ = maps.shape
-    out = np.empty((n, M))
-    for s in range(M):
-        out[:, s] = np.diagonal(maps, offset=s, axis1=1, axis2=2).mean(axis=1)
+    smax = M if smax is None else min(M, smax)
+    out = np.empty((n, smax))
+    i = np.arange(M)
+    for s in range(smax):
+        out[:, s] = maps[:, i[:M - s], i[s:]].mean(axis=1, dtype=np.float64)
     return out
+
+
+def powerlaw_map(maps, bins=None):
+    """The P(s)-only predictor: a power law P(s) = a s^b fitted (least squares
+    in log-log) to the mean P(s) of `maps` over s = 1 .. bins/2 - 1, spread
+    over every bin pair |i - j| = s, with the mean's own P(0) on the diagonal.
+    Returns one map [1][bins][bins]."""
+    ps = ps_curve(maps).mean(axis=0)
+    M = ps.shape[0] if bins is None else bins
+    s = np.arange(1, M // 2)
+    b, loga = np.polyfit(np.log(s), np.log(np.maximum(ps[s], 1e-12)), 1)
+    d = np.abs(np.arange(M)[:, None] - np.arange(M)[None, :]).astype(np.float64)
+    m = np.exp(loga) * np.maximum(d, 1.0) ** b
+    np.fill_diagonal(m, ps[0])
+    return m[None].astype(np.float32)
 
 
 def ps_log_bins(maps):
     """P(s) averaged over octaves of separation, s in [1, 2), [2, 4), ...,
     [bins/4, bins/2): one value per octave and map."""
-    ps = ps_curve(maps)
-    M = ps.shape[1]
+    M = np.asarray(maps).shape[1]
+    ps = ps_curve(maps, M // 2)
     out, a = [], 1
     while a < M // 2:
         b = min(2 * a, M // 2)
