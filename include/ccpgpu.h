@@ -54,6 +54,8 @@ typedef struct ccpgpu_info {
   float dt, kT, noise_sd;
   float contact_cutoff;
   int32_t frames_observed;
+  int32_t persistent_reach; /* 0: graph path; 1 or 2: steps run in the
+                               persistent per-system kernel with that stencil */
 } ccpgpu_info;
 
 typedef struct ccpgpu_system_info {

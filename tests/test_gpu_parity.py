@@ -292,14 +292,17 @@ def test_observables_match_oracle(ccp_sim, orc):
     assert abs(got[4 + 128:].sum() - want[4 + 128:].sum()) < 1e-3 * want[4 + 128:].sum()
 
 
-def test_trajectory_matches_oracle_1000_steps(engine_lib, orc):
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_trajectory_matches_oracle_1000_steps(engine_lib, orc, persistent):
     """Same seed, same Philox stream, same start: 1000 Heun steps on the GPU vs
-    the FP64 oracle. Stated drift: max |dr| < 2e-3 sigma (FP32 rounding
-    amplified by the chaotic dynamics)."""
+    the FP64 oracle, on the graph path and on the persistent per-system
+    kernel. Stated drift: max |dr| < 2e-3 sigma (FP32 rounding amplified by
+    the chaotic dynamics)."""
     from tfm_gb300.ccpgpu import ChrSim
 
     txt, R, n_l = ccp_params(1024, laf=0.3)
-    sim = ChrSim(txt, seed=1234)
+    sim = ChrSim(txt + "persistent %d\n" % persistent, seed=1234)
+    assert (sim.info().persistent_reach > 0) == bool(persistent)
     sim.generate_initial_condition()
     x0 = sim.positions()
     pt = sim.types()
@@ -317,13 +320,16 @@ def test_trajectory_matches_oracle_1000_steps(engine_lib, orc):
     assert drift.max() < 2e-3
 
 
-def test_trajectory_baseline_matches_oracle_1000_steps(engine_lib, orc):
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_trajectory_baseline_matches_oracle_1000_steps(engine_lib, orc, persistent):
     """The same for the baseline force field (Lennard-Jones A-A attraction,
     WCA, lamina sites, the displacement cap) on its default typed pair
-    kernel: 1000 Heun steps vs the FP64 oracle, max |dr| < 2e-3 sigma."""
+    kernel and on the persistent kernel: 1000 Heun steps vs the FP64 oracle,
+    max |dr| < 2e-3 sigma."""
     from tfm_gb300.ccpgpu import ChrSim
 
-    sim = ChrSim(baseline_params(1024), seed=4321)
+    sim = ChrSim(baseline_params(1024, "persistent %d\n" % persistent), seed=4321)
+    assert (sim.info().persistent_reach > 0) == bool(persistent)
     assert "pair_kernel" not in baseline_params(1024)  # the preset's default (typed)
     sim.generate_initial_condition()
     x0, pt, lbs = sim.positions(), sim.types(), sim.lbs()

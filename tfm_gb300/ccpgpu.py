@@ -59,7 +59,8 @@ class Info(C.Structure):
                 ("frames_per_file", C.c_uint32), ("steps_per_frame", C.c_uint32),
                 ("frame_index", C.c_uint32), ("time", C.c_float), ("step", C.c_uint64),
                 ("dt", C.c_float), ("kT", C.c_float), ("noise_sd", C.c_float),
-                ("contact_cutoff", C.c_float), ("frames_observed", C.c_int32)]
+                ("contact_cutoff", C.c_float), ("frames_observed", C.c_int32),
+                ("persistent_reach", C.c_int32)]
 
 
 class SystemInfo(C.Structure):

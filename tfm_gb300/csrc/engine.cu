@@ -28,6 +28,7 @@
 #include "analysis.h"
 #include "host.h"
 #include "kernels.cuh"
+#include "persist.cuh"
 
 namespace ccpgpu {
 
@@ -162,6 +163,10 @@ struct Engine {
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
   std::map<std::tuple<int, int, int>, uint64_t> graph_kernels;  // kernel nodes per graph
   uint64_t kcount = 0;  // engine kernels launched (graph nodes included)
+  // persistent per-system path (persist.cuh): 0 when the batch does not use it
+  int persist_reach = 0;
+  size_t persist_bytes = 0;
+  DevBuf<PGrid> d_pgrid;
 
   ~Engine() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
@@ -338,7 +343,79 @@ struct Engine {
     CK(cudaMemsetAsync(sorted.p, 0, sizeof(float4) * (nb + 1), stream));
     CK(cudaMemsetAsync(lbs_start.p, 0, sizeof(uint32_t) * (nc + 1), stream));
     reset_observables();
+    setup_persist();
     CK(cudaStreamSynchronize(stream));
+  }
+
+  // Shared-memory cell grids of the persistent path: cells of the largest
+  // pair cutoff over 2 (5x5x5 stencil) when every system then fits one CTA's
+  // shared memory, else cells of the cutoff (3x3x3), else the path is off.
+  void setup_persist() {
+    persist_reach = 0;
+    persist_bytes = 0;
+    if (!par.persistent) return;
+    int dev = 0, optin = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t limit = (size_t)optin - 1024;  // the scan's static shared words
+    // a margin above the cutoff keeps pairs at it within the stencil despite
+    // the rounding of the cell coordinates
+    const float rc = std::max({ff.rc_att, ff.rc_rep, ff.rc_icg}) * 1.0001f;
+    const int ns = (int)hsys.size();
+    for (int reach = 2; reach >= 1; --reach) {
+      std::vector<PGrid> g(ns);
+      size_t bytes = 0;
+      bool ok = true;
+      for (int s = 0; s < ns && ok; ++s) {
+        const float csl = rc / (float)reach;
+        const float half = std::ceil(geo[s].d_m / csl);
+        if (!(half <= 64.0f) || hsys[s].n > 65535) {
+          ok = false;
+          break;
+        }
+        const int cps = std::max(2, 2 * (int)half);
+        g[s] = PGrid{cps, 1.0f / csl, cps * cps * cps, 0};
+        bytes = std::max(bytes, persist_smem_bytes(hsys[s].n, g[s].n_cells));
+        ok = bytes <= limit;
+      }
+      if (!ok) continue;
+      d_pgrid.alloc(ns);
+      CK(cudaMemcpyAsync(d_pgrid.p, g.data(), sizeof(PGrid) * ns, cudaMemcpyHostToDevice, stream));
+      if (reach == 2) {
+        CK(cudaFuncSetAttribute(k_persist<MODE_DST, 2>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        CK(cudaFuncSetAttribute(k_persist<MODE_ICG, 2>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      } else {
+        CK(cudaFuncSetAttribute(k_persist<MODE_DST, 1>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        CK(cudaFuncSetAttribute(k_persist<MODE_ICG, 1>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      }
+      persist_reach = reach;
+      persist_bytes = bytes;
+      return;
+    }
+  }
+
+  // g Heun steps of every system in one launch (one CTA per system).
+  void launch_persist(int mode, int g) {
+    const unsigned ns = (unsigned)hsys.size();
+    const unsigned long long s0 = (unsigned long long)step;
+#define CCPGPU_PERSIST(M, R)                                                              \
+  k_persist<M, R><<<ns, PERSIST_THREADS, persist_bytes, stream>>>(                        \
+      d_sys.p, d_pgrid.p, ff, pos.p, lbs_sorted.p, lbs_start.p, s0, g, d_err.p)
+    if (mode == MODE_DST && persist_reach == 2)
+      CCPGPU_PERSIST(MODE_DST, 2);
+    else if (mode == MODE_DST)
+      CCPGPU_PERSIST(MODE_DST, 1);
+    else if (persist_reach == 2)
+      CCPGPU_PERSIST(MODE_ICG, 2);
+    else
+      CCPGPU_PERSIST(MODE_ICG, 1);
+#undef CCPGPU_PERSIST
+    CK(cudaGetLastError());
+    kcount += 1;
   }
 
   void build_tiles() {
@@ -944,6 +1021,10 @@ struct Engine {
   // n steps of the given mode; observation every obs_every steps (DST only).
   void run_steps(uint64_t n, int mode, uint32_t obs_every) {
     if (!positions_valid) throw Error(ST_STATE, "positions not initialised");
+    if (persist_reach > 0) {
+      run_steps_persist(n, mode, obs_every);
+      return;
+    }
     set_device_step();
     const int chunk = 128;
     uint64_t left = n;
@@ -969,6 +1050,36 @@ struct Engine {
       dev_next += g;
       left -= g;
     }
+  }
+
+  // The persistent path: per chunk (a frame, at most 512 steps) the
+  // observation of its first state when due (as the graph path's first step
+  // does), one launch of the persistent kernel, and the cell histogram of the
+  // new positions that the next sort and observation expect.
+  void run_steps_persist(uint64_t n, int mode, uint32_t obs_every) {
+    uint64_t left = n;
+    while (left > 0) {
+      int g;
+      bool obs = false;
+      if (mode == MODE_DST && obs_every > 0) {
+        uint64_t to_next = (obs_every - (step % obs_every)) % obs_every;
+        obs = to_next == 0;
+        g = (int)std::min<uint64_t>(left, obs ? obs_every : to_next);
+      } else {
+        g = (int)std::min<uint64_t>(left, 512);
+      }
+      g = std::min(g, 512);
+      if (obs) {
+        sort_now();
+        launch_observe_sorted(false);
+        ++frames_observed;
+      }
+      launch_persist(mode, g);
+      recount();
+      step += g;
+      left -= g;
+    }
+    dev_next = ~0ull;  // the device step counter was not advanced
   }
 
   void sync_and_check() {
@@ -1452,6 +1563,7 @@ int ccpgpu_info_get(const ccpgpu_sim *h, ccpgpu_info *o) {
     o->noise_sd = e.ff.sd;
     o->contact_cutoff = e.par.contact_cutoff;
     o->frames_observed = e.frames_observed;
+    o->persistent_reach = e.persist_reach;
   });
 }
 

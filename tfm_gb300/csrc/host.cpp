@@ -217,6 +217,8 @@ Params parse_params(const std::string &text) {
   p.pair_lanes = pm.get<int>("pair_lanes", 0);  // 0: by the batch's bead count
   if (!(p.pair_lanes == 0 || p.pair_lanes == 1 || p.pair_lanes == 2 || p.pair_lanes == 4))
     fail("pair_lanes out of range");
+  p.persistent = pm.get<int>("persistent", 0);
+  if (!(p.persistent == 0 || p.persistent == 1)) fail("persistent out of range");
   if (!(p.n_chains >= 1 && (uint32_t)p.n_chains <= p.N)) fail("number_of_chains out of range");
   if (!(p.contact_cutoff > 0.0f)) fail("contact_cutoff out of range");
   if (p.contact_bins < 0) fail("contact_bins out of range");

@@ -76,6 +76,9 @@ struct Params {
   // 2: half shell (Newton's third law), thread per bead
   int pair_kernel = 2;
   int pair_lanes = 0;  // lanes per bead of the half-shell pair kernels (0: by bead count)
+  // 1: when every system fits one CTA's shared memory, steps run in the
+  // persistent per-system kernel (one launch per frame); 0: graph path
+  int persistent = 0;
   std::string sequence_file = "Program/data/sequence.txt";
   ForceField ff{};
 };

@@ -1104,24 +1104,27 @@ __device__ __forceinline__ float3 lbs_force(float4 x, const SysDesc &s, const Fo
   return f;
 }
 
-// Bonded (elastic + bending) force on bead i of X (chrsim.cu:13-76). Bonds
-// exist only inside a chain; BF_START marks chain heads.
-__device__ __forceinline__ float3 bonded_force(const float4 *__restrict__ X, int i, float4 xi,
-                                               int end, const ForceField &ff) {
+// Bonded (elastic + bending) force on bead i (chrsim.cu:13-76). Bonds exist
+// only inside a chain; BF_START marks chain heads. The chain neighbours are
+// read through X(j): a chain-order array, or a cell-ordered copy through a
+// slot map; the flags are the low bits of each position's w word.
+template <class Load>
+__device__ __forceinline__ float3 bonded_force_at(Load X, int i, float4 xi, int end,
+                                                  const ForceField &ff) {
   uint32_t fi = wbits(xi);
   float4 xm1 = xi, xm2 = xi, xp1 = xi, xp2 = xi;
   bool e1 = (fi & BF_START) == 0u;  // bond (i-1, i)
   bool e0 = false, e2 = false, e3 = false;
   if (e1) {
-    xm1 = X[i - 1];
+    xm1 = X(i - 1);
     e0 = (wbits(xm1) & BF_START) == 0u;  // bond (i-2, i-1)
-    if (e0) xm2 = X[i - 2];
+    if (e0) xm2 = X(i - 2);
   }
   if (i + 1 < end) {
-    xp1 = X[i + 1];
+    xp1 = X(i + 1);
     e2 = (wbits(xp1) & BF_START) == 0u;  // bond (i, i+1)
     if (e2 && i + 2 < end) {
-      xp2 = X[i + 2];
+      xp2 = X(i + 2);
       e3 = (wbits(xp2) & BF_START) == 0u;  // bond (i+1, i+2)
     }
   }
@@ -1168,6 +1171,11 @@ __device__ __forceinline__ float3 bonded_force(const float4 *__restrict__ X, int
     f.z += ff.k_b * (c_v0 * v0.z + c_v1 * v1.z + c_v2 * v2.z + c_v3 * v3.z);
   }
   return f;
+}
+
+__device__ __forceinline__ float3 bonded_force(const float4 *__restrict__ X, int i, float4 xi,
+                                               int end, const ForceField &ff) {
+  return bonded_force_at([X](int j) { return X[j]; }, i, xi, end, ff);
 }
 
 // Deterministic displacement of one stage limited to max_step (> 0): keeps the
