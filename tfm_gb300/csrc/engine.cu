@@ -8,7 +8,8 @@
 //   sorted           float4 per bead in cell order: x, y, z, (index << 3 | flags)
 //   fs               float4 per bead in cell order: pair force
 //   rank             uint32 per bead: rank of the bead inside its cell
-//   counts, start    uint32 per cell (+1): histogram and exclusive prefix
+//   counts           uint8 per cell: histogram (four cells per 32-bit word)
+//   start            uint32 per cell (+1): exclusive prefix
 // Cells of system s occupy [cell_off, cell_off + cps^3); because every system
 // lives in its own cells, the counting sort keeps each system's beads inside
 // its own slot range [bead_off, bead_off + n).
@@ -298,7 +299,7 @@ struct Engine {
     fout.alloc(nb + 1);
     rank.alloc(nb + 1);
     size_t cpad = (size_t)nblk * SCAN_CHUNK;
-    counts.alloc(cpad);
+    counts.alloc(cpad / 4);  // byte counts
     start.alloc(cpad + 4);
     bsum.alloc(nblk + 1);
     lbs_sorted.alloc(std::max(nl, 1));
@@ -332,7 +333,7 @@ struct Engine {
     CK(cudaMemcpyAsync(d_chain_len.p, chain_len.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_chain_ps_off.p, chain_ps_off.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_chain_smax.p, chain_smax.data(), 4 * nch, cudaMemcpyHostToDevice, stream));
-    CK(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * cpad, stream));
+    CK(cudaMemsetAsync(counts.p, 0, cpad, stream));
     CK(cudaMemsetAsync(start.p, 0, sizeof(uint32_t) * (cpad + 4), stream));
     CK(cudaMemsetAsync(d_err.p, 0, sizeof(int) * ERR_COUNT, stream));
     CK(cudaMemsetAsync(pos.p, 0, sizeof(float4) * (nb + 1), stream));
@@ -439,7 +440,9 @@ struct Engine {
 
   // Uploads positions + flags (through pinned staging) and rebuilds the cell
   // histogram of pos.
-  void upload_positions() {
+  // count = false: the positions are placeholders about to be overwritten
+  // (they would all fall into one cell), so no histogram is built.
+  void upload_positions(bool count = true) {
     set_chain_flags();
     float4 *v = pin_up;
     for (int i = 0; i < nb; ++i) {
@@ -453,7 +456,7 @@ struct Engine {
     std::memcpy(&wsf, &ws, 4);
     v[nb] = make_float4(0, 0, 0, wsf);
     CK(cudaMemcpyAsync(pos.p, v, sizeof(float4) * (nb + 1), cudaMemcpyHostToDevice, stream));
-    recount();
+    if (count) recount();
     CK(cudaStreamSynchronize(stream));
     positions_valid = true;
     flags_current = true;
@@ -475,7 +478,7 @@ struct Engine {
   }
 
   void recount() {
-    CK(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * (size_t)nblk * SCAN_CHUNK, stream));
+    CK(cudaMemsetAsync(counts.p, 0, (size_t)nblk * SCAN_CHUNK, stream));
     k_count<<<(unsigned)htiles.size(), tile, 0, stream>>>(d_tiles.p, d_sys.p, pos.p, counts.p,
                                                            rank.p, d_err.p);
     CK(cudaGetLastError());
@@ -550,7 +553,7 @@ struct Engine {
   void launch_scatter(const float4 *src) {
     k_scatter<<<(unsigned)htiles.size(), tile, 0, stream>>>(
         d_tiles.p, d_sys.p, src, rank.p, start.p, sorted.p,
-        par.pair_kernel >= 2 ? fs.p : nullptr, d_err.p);
+        par.pair_kernel >= 2 ? fs.p : nullptr, counts.p, d_err.p);
     kcount += 1;
   }
 
@@ -822,7 +825,7 @@ struct Engine {
     build_tiles();
     nblk = (nc + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK;
     size_t cpad = (size_t)nblk * SCAN_CHUNK;
-    counts.alloc(cpad);
+    counts.alloc(cpad / 4);  // byte counts
     start.alloc(cpad + 4);
     bsum.alloc(nblk + 1);
     lbs_start.alloc(nc + 1);
@@ -1278,7 +1281,7 @@ struct Engine {
   // given, receives each chain's number of attempts.
   void random_walk(uint32_t *draws) {
     std::fill(hxyz.begin(), hxyz.end(), 0.0f);
-    upload_positions();  // flags; the walk overwrites every position
+    upload_positions(false);  // flags; the walk overwrites every position, then counts
     std::vector<WalkChain> wc((size_t)nch);
     for (size_t s = 0; s < hsys.size(); ++s) {
       const SysDesc &d = hsys[s];
@@ -2172,7 +2175,7 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
     k_scan_reduce<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum);
     k_scan_top<<<1, SCAN_TOP_THREADS, 0, s>>>(bsum, nblk, step, 0);
     k_scan_apply<<<nblk, SCAN_THREADS, 0, s>>>(counts, bsum, start, nc, nblk);
-    k_scatter<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, rank, start, sorted, fs, err);
+    k_scatter<<<n_tiles, TILE, 0, s>>>(tiles, sys, pos, rank, start, sorted, fs, counts, err);
     k_pair_half<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, sorted, start, fs);
     k_total_force<MODE_DST><<<n_tiles, TILE, 0, s>>>(tiles, sys, ff, pos, fs, rank, nullptr,
                                                      nullptr, fout);

@@ -3,7 +3,8 @@
 // One Heun step (ccp's stochastic Runge-Kutta, chrsim.cu:365-416) is
 //   [scan -> scatter(r) -> pair -> update<1>] [scan -> scatter(er) -> pair -> update<2>]
 // where
-//   scan     turns per-cell bead counts into cell start offsets (3 launches),
+//   scan     turns per-cell bead counts (one byte per cell) into cell start
+//            offsets (3 launches),
 //   scatter  writes every bead into cell order (the sorted float4 copy),
 //   pair     evaluates the excluded-volume / attraction forces over the
 //            27-cell neighbourhood in cell order (chrsim.cu:224-317),
@@ -311,6 +312,18 @@ __device__ __forceinline__ float3 bead_noise(uint32_t bead, uint64_t step, uint3
 
 // ------------------------------------------------------------------ count
 
+// Cell histograms hold one byte per cell, four cells to a 32-bit word, so the
+// scan reads one byte per cell. A cell of side ~ sigma holds a few beads; one
+// that would pass 255 sets ERR_SLOT (the carry has spoiled its neighbour's
+// count) and the run reports an inconsistent cell list. Returns the bead's
+// rank in its cell.
+__device__ __forceinline__ uint32_t cell_add(uint32_t *counts, int c, int *err) {
+  const uint32_t sh = 8u * ((uint32_t)c & 3u);
+  const uint32_t r = (atomicAdd(&counts[c >> 2], 1u << sh) >> sh) & 0xFFu;
+  if (r == 0xFFu) set_err(err, ERR_SLOT);
+  return r;
+}
+
 // Cell histogram of the current positions: rank[i] = position of bead i in
 // its cell, counts[c] += 1. Used after positions are (re)loaded; during
 // stepping the update kernel does this for the position it writes.
@@ -324,7 +337,7 @@ __global__ void k_count(const Tile *__restrict__ tiles, const SysDesc *__restric
   bool esc = false;
   float4 p = pos[i];
   int c = bead_cell(p, s, esc);
-  rank[i] = atomicAdd(&counts[c], 1u);
+  rank[i] = cell_add(counts, c, err);
   if (esc) set_err(err, ERR_ESCAPE);
 }
 
@@ -361,18 +374,15 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total)
   return r;
 }
 
-// Phase 1: per-CTA totals of SCAN_CHUNK cells. counts is padded to a multiple
-// of SCAN_CHUNK (zeros beyond n_cells).
+// Phase 1: per-CTA totals of SCAN_CHUNK cells (SCAN_ITEMS = 16 byte counts,
+// one 16-byte load, per thread). counts is padded to a multiple of
+// SCAN_CHUNK cells (zeros beyond n_cells).
 __global__ void __launch_bounds__(SCAN_THREADS)
     k_scan_reduce(const uint32_t *__restrict__ counts, uint32_t *__restrict__ block_sums) {
-  const uint4 *c4 = reinterpret_cast<const uint4 *>(counts) +
-                    (size_t)blockIdx.x * (SCAN_CHUNK / 4) + threadIdx.x * (SCAN_ITEMS / 4);
-  uint32_t v = 0;
-#pragma unroll
-  for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
-    uint4 q = c4[k];
-    v += q.x + q.y + q.z + q.w;
-  }
+  static_assert(SCAN_ITEMS == 16, "one uint4 of byte counts per thread");
+  const uint4 q = reinterpret_cast<const uint4 *>(counts)[(size_t)blockIdx.x * SCAN_THREADS +
+                                                         threadIdx.x];
+  uint32_t v = __vsadu4(q.x, 0u) + __vsadu4(q.y, 0u) + __vsadu4(q.z, 0u) + __vsadu4(q.w, 0u);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __shared__ uint32_t ws[SCAN_THREADS / 32];
@@ -406,29 +416,21 @@ __global__ void __launch_bounds__(SCAN_TOP_THREADS)
   }
 }
 
-// Phase 3: cell start offsets (exclusive scan), start[n_cells] = total, and
-// the counts are cleared for the next histogram.
+// Phase 3: cell start offsets (exclusive scan), start[n_cells] = total. The
+// counts stay: the scatter clears each occupied cell's byte as it reads the
+// cell, so the next histogram starts from zero without a pass over all cells.
 __global__ void __launch_bounds__(SCAN_THREADS)
-    k_scan_apply(uint32_t *__restrict__ counts, const uint32_t *__restrict__ block_sums,
+    k_scan_apply(const uint32_t *__restrict__ counts, const uint32_t *__restrict__ block_sums,
                  uint32_t *__restrict__ start, int n_cells, int nb) {
-  uint4 *c4 = reinterpret_cast<uint4 *>(counts) + (size_t)blockIdx.x * (SCAN_CHUNK / 4) +
-              threadIdx.x * (SCAN_ITEMS / 4);
+  const uint4 q = reinterpret_cast<const uint4 *>(counts)[(size_t)blockIdx.x * SCAN_THREADS +
+                                                         threadIdx.x];
+  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
   uint32_t v[SCAN_ITEMS];
-#pragma unroll
-  for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
-    uint4 q = c4[k];
-    v[4 * k + 0] = q.x;
-    v[4 * k + 1] = q.y;
-    v[4 * k + 2] = q.z;
-    v[4 * k + 3] = q.w;
-    c4[k] = make_uint4(0u, 0u, 0u, 0u);
-  }
   uint32_t tsum = 0;
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; ++k) {
-    uint32_t x = v[k];
     v[k] = tsum;
-    tsum += x;
+    tsum += (w[k >> 2] >> (8 * (k & 3))) & 0xFFu;
   }
   __shared__ uint32_t tot;
   uint32_t off = block_excl_scan<SCAN_THREADS>(tsum, &tot) + block_sums[blockIdx.x];
@@ -445,11 +447,13 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 // Counting-sort scatter: bead i goes to slot start[cell] + rank[i] of the
 // cell-ordered copy, with its global index packed above the flag bits; the
 // slot replaces the rank in rank[i], so the passes that read the pair force
-// back in chain order (update, total force) need no cell lookup.
+// back in chain order (update, total force) need no cell lookup. The cell's
+// byte count is cleared for the next histogram (the scan has consumed it).
 __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restrict__ sys,
                           const float4 *__restrict__ src, uint32_t *__restrict__ rank,
                           const uint32_t *__restrict__ start, float4 *__restrict__ sorted,
-                          float4 *__restrict__ fs_clear, int *__restrict__ err) {
+                          float4 *__restrict__ fs_clear, uint32_t *__restrict__ counts,
+                          int *__restrict__ err) {
   Tile t = tiles[blockIdx.x];
   const SysDesc &s = sys[t.sys];
   int i = t.begin + threadIdx.x;
@@ -459,6 +463,7 @@ __global__ void k_scatter(const Tile *__restrict__ tiles, const SysDesc *__restr
   bool esc = false;
   float4 p = src[i];
   int c = bead_cell(p, s, esc);
+  reinterpret_cast<uint8_t *>(counts)[c] = 0;
   uint32_t slot = start[c] + rank[i];
   if (slot < (uint32_t)s.bead_off || slot >= (uint32_t)end) {
     set_err(err, ERR_SLOT);
@@ -1276,7 +1281,7 @@ __global__ void __launch_bounds__(256, 7)
   if (!(isfinite(out.x) && isfinite(out.y) && isfinite(out.z))) set_err(err, ERR_NAN);
   bool esc2 = false;
   int c_new = bead_cell(out, s, esc2);
-  rank[i] = atomicAdd(&counts[c_new], 1u);
+  rank[i] = cell_add(counts, c_new, err);
   if (esc2) set_err(err, ERR_ESCAPE);
 }
 
