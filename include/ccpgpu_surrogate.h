@@ -96,6 +96,11 @@ int ccpsur_train_step(ccpsur_net *h, const int32_t *rows, int32_t n, double *los
  * host memory (any n; processed in batches). */
 int ccpsur_predict(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int32_t n, float *maps);
 
+/* The contact probability by bin separation of the predicted maps,
+ * ps[n][bins] (ps[k][s] = the mean of the map's diagonal s), reduced on the
+ * device: what screening needs, without copying every map to the host. */
+int ccpsur_predict_ps(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int32_t n, float *ps);
+
 /* The same for dataset rows; maps may be NULL (the result stays on the
  * device, for timing). */
 int ccpsur_predict_rows(ccpsur_net *h, const int32_t *rows, int32_t n, float *maps);

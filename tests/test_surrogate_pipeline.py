@@ -93,7 +93,11 @@ def test_screen_resimulates_random_and_out_of_envelope(engine_lib):
         net.set_dataset(types, lad, maps)
         S.train(net, 64, 3, seed=1)
         rep, fb = S.screen(net, st, sl, env, 0.01, seed=3, sim=counting_sim, chunk=256)
-        pb = S.ps_log_bins(net.predict(st, sl))
+        maps_pred = net.predict(st, sl)
+        pb = S.ps_log_bins(maps_pred)
+        # the device-side P(s) equals the host reduction of the same maps
+        ps_dev = net.predict_ps(st, sl)
+        assert np.allclose(ps_dev, S.ps_curve(maps_pred), rtol=1e-5, atol=1e-9)
         assert net.error_flags() == 0
     lo, hi = env
     out = np.any((pb < lo) | (pb > hi), axis=1)

@@ -361,6 +361,7 @@ struct Net {
   std::vector<Buf<bf16>> h, z;             // h[1..enc_layers], z[0..head_layers]
   std::vector<Buf<uint32_t>> emask, hmask;  // emask[1..], hmask[1..]
   Buf<float> y, pred, dyb, dist_part;
+  Buf<float> ps_dev;  // P(s) of one batch's predicted maps (predict_ps)
   Buf<uint8_t> decay;
   // backward
   Buf<float> hdz[2], edz[2], dhp;
@@ -982,6 +983,32 @@ int ccpsur_predict(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int3
       n.predict_out(b, maps, first);
     }
     n.drain_maps();
+    n.check_flags();
+  });
+}
+
+int ccpsur_predict_ps(ccpsur_net *h, const uint8_t *types, const uint8_t *lad, int32_t cnt,
+                      float *ps) {
+  return sguard([&] {
+    Net &n = net_of(h);
+    sneed(types && ps && cnt >= 0, "null argument");
+    const size_t L = n.L;
+    const int M = n.M;
+    if (n.ps_dev.n < (size_t)n.cfg.batch * M) n.ps_dev.alloc((size_t)n.cfg.batch * M);
+    n.discard_pending();
+    for (int32_t first = 0; first < cnt; first += n.cfg.batch) {
+      const int b = std::min(n.cfg.batch, cnt - first);
+      SCK(cudaMemcpyAsync(n.in_types.p, types + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
+      if (lad)
+        SCK(cudaMemcpyAsync(n.in_lad.p, lad + (size_t)first * L, (size_t)b * L, cudaMemcpyHostToDevice, n.st));
+      n.forward(n.in_types.p, lad ? n.in_lad.p : nullptr, nullptr, b, false);
+      n.predict_out(b, nullptr, first);
+      k_ps_curve<<<b, 256, 0, n.st>>>(n.pred.p, M, n.ps_dev.p);
+      SCK(cudaGetLastError());
+      ++n.run.kernels;
+      SCK(cudaMemcpyAsync(ps + (size_t)first * M, n.ps_dev.p, sizeof(float) * (size_t)b * M,
+                          cudaMemcpyDeviceToHost, n.st));
+    }
     n.check_flags();
   });
 }

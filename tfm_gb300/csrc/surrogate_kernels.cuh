@@ -695,6 +695,18 @@ __global__ void k_predict_maps(const float *__restrict__ y, int M, int n, float 
   out[k] = expf(fminf(yh, YHAT_MAX));
 }
 
+// P(s) of predicted maps: block b reduces map b, thread s (strided) the mean
+// of its diagonal s, pred[b][i][i + s] for i < M - s, summed in FP64.
+__global__ void __launch_bounds__(256)
+    k_ps_curve(const float *__restrict__ pred, int M, float *__restrict__ ps) {
+  const float *m = pred + (size_t)blockIdx.x * M * M;
+  for (int s = threadIdx.x; s < M; s += blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i + s < M; ++i) acc += (double)m[(size_t)i * M + i + s];
+    ps[(size_t)blockIdx.x * M + s] = (float)(acc / (double)(M - s));
+  }
+}
+
 // Loss and the gradient entering the head. yhat = (y + y^T) / 2 and the
 // Poisson deviance of the observed contact probability p against exp(yhat),
 // weighted per separation s = |i - j| by w[s] (the inverse of the dataset's

@@ -26,7 +26,8 @@ from . import ccpgpu
 SYMBOLS = (
     "ccpsur_create", "ccpsur_destroy", "ccpsur_info_get", "ccpsur_get_params",
     "ccpsur_set_params", "ccpsur_get_grads", "ccpsur_set_dataset", "ccpsur_loss_grad",
-    "ccpsur_train_step", "ccpsur_predict", "ccpsur_predict_rows", "ccpsur_synchronize",
+    "ccpsur_train_step", "ccpsur_predict", "ccpsur_predict_ps", "ccpsur_predict_rows",
+    "ccpsur_synchronize",
     "ccpsur_stream_handle", "ccpsur_error_flags", "ccpsur_kernel_count", "ccpsur_conv_bf16",
     "ccpsur_wgrad_bf16",
 )
@@ -60,6 +61,7 @@ def load():
         "ccpsur_loss_grad": [P, P, I32, C.POINTER(C.c_double)],
         "ccpsur_train_step": [P, P, I32, C.POINTER(C.c_double)],
         "ccpsur_predict": [P, P, P, I32, P],
+        "ccpsur_predict_ps": [P, P, P, I32, P],
         "ccpsur_predict_rows": [P, P, I32, P],
         "ccpsur_synchronize": [P],
         "ccpsur_stream_handle": [P, C.POINTER(P)],
@@ -212,6 +214,15 @@ class Surrogate:
         _check(_lib.ccpsur_predict(self._h, _ptr(t), _ptr(l), t.shape[0], _ptr(out)))
         return out
 
+    def predict_ps(self, types, lad=None):
+        """P(s) [n][bins] of the predicted maps (the mean of each diagonal),
+        reduced on the device: no map is copied to the host."""
+        t = np.ascontiguousarray(types, np.uint8)
+        l = None if lad is None else np.ascontiguousarray(lad, np.uint8)
+        out = np.empty((t.shape[0], self.info().bins), np.float32)
+        _check(_lib.ccpsur_predict_ps(self._h, _ptr(t), _ptr(l), t.shape[0], _ptr(out)))
+        return out
+
     def predict_rows(self, rows, copy=True):
         r = np.ascontiguousarray(rows, np.int32)
         out = None
@@ -326,17 +337,23 @@ def powerlaw_map(maps, bins=None):
     return m[None].astype(np.float32)
 
 
+def ps_octaves(ps, bins):
+    """Octave means of P(s) curves ps [n][>= bins/2]: s in [1, 2), [2, 4), ...,
+    [bins/4, bins/2), one value per octave and curve."""
+    ps = np.asarray(ps, np.float64)
+    out, a = [], 1
+    while a < bins // 2:
+        b = min(2 * a, bins // 2)
+        out.append(ps[:, a:b].mean(axis=1))
+        a = b
+    return np.stack(out, axis=1)
+
+
 def ps_log_bins(maps):
     """P(s) averaged over octaves of separation, s in [1, 2), [2, 4), ...,
     [bins/4, bins/2): one value per octave and map."""
     M = np.asarray(maps).shape[1]
-    ps = ps_curve(maps, M // 2)
-    out, a = [], 1
-    while a < M // 2:
-        b = min(2 * a, M // 2)
-        out.append(ps[:, a:b].mean(axis=1))
-        a = b
-    return np.stack(out, axis=1)
+    return ps_octaves(ps_curve(maps, M // 2), M)
 
 
 def ps_error(pred, ref):
@@ -382,7 +399,8 @@ def envelope(maps, margin=0.25):
 
 
 def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
-    """Batched inference over many sequences with a simulation fallback: a
+    """Batched inference over many sequences with a simulation fallback
+    (only each prediction's P(s) comes back from the device): a
     random `fallback_fraction` of them, plus every sequence whose predicted
     P(s) leaves the envelope in some separation octave, is re-simulated by
     `sim` (a callable (types, lad) -> maps), whose maps check the prediction.
@@ -395,9 +413,10 @@ def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
     out_env = np.zeros(n, bool)
     pb_pred = None
     t0 = time.perf_counter()
+    bins = net.info().bins
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
-        pb = ps_log_bins(net.predict(types[a:b], lad[a:b]))
+        pb = ps_octaves(net.predict_ps(types[a:b], lad[a:b]), bins)
         if pb_pred is None:
             pb_pred = np.empty((n, pb.shape[1]))
         pb_pred[a:b] = pb
@@ -416,6 +435,7 @@ def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
         "sequences": int(n),
         "predict_s": t_pred,
         "maps_per_s_with_host_io": n / t_pred,
+        "host_io": "sequences in, P(s) of every predicted map out (reduced on the device)",
         "fallback_random": int(k),
         "fallback_out_of_envelope": int(out_env.sum()),
         "simulated": int(len(fb)),
