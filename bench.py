@@ -773,6 +773,54 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, truth_reps, scr
     return rep
 
 
+def persistent_compare(profile_only=False):
+    """ms per Heun step and bead-steps/s of the graph path (`persistent 0`)
+    and the persistent per-system kernel (`persistent 1`) on single systems
+    and batches of small systems (baseline field), one JSON line per
+    workload. profile_only: just 4 x 2048 beads on the persistent kernel,
+    two launches of 20 steps (a small case for profiler captures)."""
+    from tfm_gb300.ccpgpu import Batch
+
+    text = "force_field baseline\ncontact_bins 256\nsteps_per_frame 100\n"
+    if profile_only:
+        # the start comes from the graph path, so every persistent launch is
+        # a dynamics launch (the relaxation would run on it too)
+        a = Batch(text, [2048] * 4, seeds=[1, 2, 3, 4])
+        a.generate_initial_condition()
+        b = Batch(text + "persistent 1\n", [2048] * 4, seeds=[1, 2, 3, 4])
+        b.set_types(a.types())
+        b.set_lbs(a.lbs())
+        b.set_positions(a.positions())
+        a.close()
+        for _ in range(2):
+            b.advance(20, 0)
+            b.synchronize()
+        b.close()
+        return
+    cases = [("one 2048-bead chain", [2048]), ("one 1024-bead chain", [1024]),
+             ("one 2900-bead chain", [2900]), ("512 x 1024 beads", [1024] * 512),
+             ("4096 x 1024 beads", [1024] * 4096)]
+    for name, sizes in cases:
+        row = {"workload": name}
+        for p in (0, 1):
+            b = Batch(text + "persistent %d\n" % p, sizes,
+                      seeds=np.arange(len(sizes), dtype=np.uint64) + 1)
+            b.generate_initial_condition()
+            row["persistent_reach_%d" % p] = b.info().persistent_reach
+            b.advance(200, 0)
+            b.synchronize()
+            n = 2000 if len(sizes) < 100 else 400
+            t0 = time.perf_counter()
+            b.advance(n, 100)
+            b.synchronize()
+            dt = time.perf_counter() - t0
+            key = "persistent" if p else "graph"
+            row[key + "_ms_per_step"] = 1e3 * dt / n
+            row[key + "_bead_steps_per_s"] = sum(sizes) * n / dt
+            b.close()
+        print(json.dumps(row), flush=True)
+
+
 def surrogate_profile_case():
     """A small surrogate workload for profiler captures: batch 16 of the
     default network (1024 beads, 256 bins), two batched predictions and one
@@ -834,6 +882,10 @@ def main():
                     help="measure the surrogate on the c3/c4 protocol instead of the engine")
     ap.add_argument("--sur-profile", action="store_true",
                     help="run only a small surrogate workload (for profiler captures)")
+    ap.add_argument("--persist-compare", action="store_true",
+                    help="time the graph path against the persistent per-system kernel")
+    ap.add_argument("--persist-profile", action="store_true",
+                    help="run only a small persistent-kernel workload (for profiler captures)")
     ap.add_argument("--sur-sequences", type=int, default=4096)
     ap.add_argument("--sur-sim-steps", type=int, default=20000)
     ap.add_argument("--sur-epochs", type=int, default=20)
@@ -842,7 +894,12 @@ def main():
                     help="batched bead-steps/s used to cost a simulated map (from the engine bench)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
-    if args.sur_profile:
+    if args.persist_compare or args.persist_profile:
+        from tfm_gb300 import build as eb
+
+        eb.build()
+        persistent_compare(profile_only=args.persist_profile)
+    elif args.sur_profile:
         from tfm_gb300 import build as eb
 
         eb.build()
