@@ -46,7 +46,7 @@ PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4
 # DRAM bytes per bead of one pair launch (dram__bytes_read.sum +
 # dram__bytes_write.sum) from an ncu capture of the typed pair kernel on this
 # workload; a constant of that capture, not measured in the timed run
-PAIR_TRAFFIC_PER_BEAD = 59.2
+PAIR_TRAFFIC_PER_BEAD = 58.9
 METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
 
 
@@ -188,81 +188,36 @@ def cpu_sample(sizes, seconds=12.0, prebuilt=None):
 
 
 # ------------------------------------------------- reference kernels on the GPU
-REF_CUBIN = os.path.join(ROOT, "oracle", "_ref", "ccp_ref.cubin")
-REF_NAMES = {  # entry names as ptxas reports them for oracle/ref/ref_kernels.cu
-    "init_ps": "_ZN3mmc7init_psEjP24curandStatePhilox4_32_10j",
-    "begin_iter": "_ZN3mmc10begin_iterEjPNS_5vec3fES1_fS1_P24curandStatePhilox4_32_10",
-    "calc_indexes": "_ZN3mmc12calc_indexesEjfjPjS0_PNS_5vec3fE",
-    "set_cells_empty": "_ZN3mmc15set_cells_emptyEjPjS0_",
-    "find_cells_limits": "_ZN3mmc17find_cells_limitsEjPjS0_S0_",
-    "exec_RK_1": "_ZN3mmc9exec_RK_1ILNS_5stypeE0EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_S6_"
-                 "S6_PNS_6sugridES8_",
-    "exec_RK_2": "_ZN3mmc9exec_RK_2ILNS_5stypeE0EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_S6_"
-                 "S6_S6_PNS_6sugridES8_",
-}
-
-
 def reference_gpu_step(sizes, reps=20):
     """ccp's own per-step kernels (chrsim.cu:572-580: begin_iter, two cell-list
     builds, exec_RK_1<DST>, exec_RK_2<DST>), compiled from the reference's
-    sources into oracle/_ref/ccp_ref.cubin, timed on this GPU with CUDA events
-    on static inputs: a relaxed configuration with ccp's force field and the
-    cell list of its positions. ccp sorts the cell keys with CUB's
-    DeviceRadixSort::SortPairs from host code, which the cubin cannot launch;
-    torch.sort(stable=True) of the same keys (CUB's radix sort as well) stands
-    in for it. Every timed launch sees the same inputs (positions are restored
-    before each exec_RK_2), so nothing can leave the cell grid. The step time
-    is the sum of the kernel times: no launch gaps, in ccp's favour."""
+    sources into oracle/_ref/ccp_ref.cubin and driven by oracle/ccp_gpu_ref.py,
+    timed on this GPU with CUDA events on static inputs: a relaxed
+    configuration with ccp's force field and the cell list of its positions,
+    on ccp's own grid (cells of aco, 2 ceil(R_n / aco) per side). ccp sorts
+    the cell keys with CUB's DeviceRadixSort::SortPairs from host code, which
+    the cubin cannot launch; torch.sort(stable=True) of the same keys (CUB's
+    radix sort as well) stands in for it. Every timed launch sees the same
+    inputs (positions are restored before each exec_RK_2), so nothing can
+    leave the cell grid. The step time is the sum of the kernel times: no
+    launch gaps, in ccp's favour."""
     import ctypes as C
 
     import torch
 
+    from oracle import ccp_gpu_ref as ref
     from oracle import oracle as orc
 
-    if not os.path.exists(REF_CUBIN):
-        return {"unavailable": "oracle/_ref/ccp_ref.cubin not built (needs the reference sources)"}
-    torch.cuda.init()
-    torch.zeros(1, device="cuda")
-    cu = C.CDLL("libcuda.so.1")
-
-    def ck(rc):
-        if rc != 0:
-            raise RuntimeError("CUDA driver error %d" % rc)
-
-    ck(cu.cuInit(0))
-    dev, ctx, mod = C.c_int(), C.c_void_p(), C.c_void_p()
-    ck(cu.cuDeviceGet(C.byref(dev), torch.cuda.current_device()))
-    ck(cu.cuDevicePrimaryCtxRetain(C.byref(ctx), dev))
-    ck(cu.cuCtxSetCurrent(ctx))
-    ck(cu.cuModuleLoad(C.byref(mod), REF_CUBIN.encode()))
-    fns = {}
-    for k, name in REF_NAMES.items():
-        f = C.c_void_p()
-        ck(cu.cuModuleGetFunction(C.byref(f), mod, name.encode()))
-        fns[k] = f
+    try:
+        mod = ref.Module()
+    except FileNotFoundError as e:
+        return {"unavailable": str(e)}
     stream = torch.cuda.current_stream()
-
-    def launch(k, n, args, tpb=128):
-        ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
-        ck(cu.cuLaunchKernel(fns[k], max((n + tpb - 1) // tpb, 1), 1, 1, tpb, 1, 1, 0,
-                             C.c_void_p(stream.cuda_stream), ptrs, None))
-
-    class CnGeom(C.Structure):  # mmc::cngeom (chrdat.cuh:48-67), plain sphere
-        _fields_ = [(k, C.c_float) for k in ("R_n", "R_o", "R_b", "noc", "boc", "nod", "bod",
-                                             "d_b", "d_m")]
-
-    class SuGrid(C.Structure):  # mmc::sugrid (sugrid.cuh:15-32)
-        _fields_ = [("n_o", C.c_uint32), ("csl", C.c_float), ("cps", C.c_uint32),
-                    ("n_c", C.c_uint32), ("uci", C.c_uint64), ("sci", C.c_uint64),
-                    ("uoi", C.c_uint64), ("soi", C.c_uint64), ("beg", C.c_uint64),
-                    ("end", C.c_uint64), ("eb", C.c_uint64), ("ebs", C.c_uint64)]
-
     P = lambda t: C.c_uint64(t.data_ptr())
-    dv = torch.device("cuda")
-    rco, aco = 1.154701, 2.0
     out = []
     rng = np.random.default_rng(11)
     for n in sizes:
+        rco = ref.RCO
         R = rco / 2 + rco / 2 * (n / 0.125) ** (1 / 3)  # ccp-profile.cu:55-62 (cvf 0.125)
         n_l = int(math.floor(0.25 * 4 / ((0.5 / (R - rco)) ** 2)))
         x = _walk(int(n), R - 0.5, rng)
@@ -273,41 +228,12 @@ def reference_gpu_step(sizes, reps=20):
                     mode=orc.MODE_ICG, prec=32).astype(np.float32)
         d = rng.normal(size=(n_l, 3))
         lbs = (d / np.linalg.norm(d, axis=1, keepdims=True) * (R - rco)).astype(np.float32)
-        ng = CnGeom(R, 0.0, 0.0, 1.0, float("nan"), R, 0.0, R, R)
-        cps = 2 * int(math.ceil(R / aco))
-        n_c = cps ** 3
-
-        def grid(pos, m):
-            t = {k: torch.zeros(max(m, 1), dtype=torch.int32, device=dv)
-                 for k in ("uci", "sci", "uoi", "soi")}
-            t["beg"] = torch.zeros(n_c, dtype=torch.int32, device=dv)
-            t["end"] = torch.zeros(n_c, dtype=torch.int32, device=dv)
-            if m:
-                launch("calc_indexes", m, [C.c_uint32(m), C.c_float(aco), C.c_uint32(cps),
-                                           P(t["uci"]), P(t["uoi"]), P(pos)])
-                keys, perm = torch.sort(t["uci"][:m], stable=True)
-                t["sci"][:m] = keys
-                t["soi"][:m] = perm.to(torch.int32)
-            launch("set_cells_empty", n_c, [C.c_uint32(n_c), P(t["beg"]), P(t["end"])])
-            if m:
-                launch("find_cells_limits", m, [C.c_uint32(m), P(t["sci"]), P(t["beg"]),
-                                                P(t["end"])])
-            g = SuGrid(m, aco, cps, n_c, *[t[k].data_ptr() for k in
-                                           ("uci", "sci", "uoi", "soi", "beg", "end")], 0, 0)
-            gd = torch.frombuffer(bytearray(bytes(g)), dtype=torch.uint8).to(dv)
-            return t, gd
-
-        r = torch.tensor(x, device=dv)
-        r0 = r.clone()
-        lr = torch.tensor(lbs if n_l else np.zeros((1, 3), np.float32), device=dv)
-        ptd = torch.tensor(pt, device=dv)
-        f, ef, er, rn = (torch.zeros((n, 3), dtype=torch.float32, device=dv) for _ in range(4))
-        ps = torch.zeros(64 * n, dtype=torch.uint8, device=dv)  # curandStatePhilox4_32_10
-        launch("init_ps", n, [C.c_uint32(n), P(ps), C.c_uint32(1)])
-        pg, pgd = grid(r, n)
-        lg, lgd = grid(lr, n_l)
+        sy = ref.System(mod, x, pt, lbs, R, seed=1, stream=stream, margin_cells=0)
+        sy.pg.build(sy.r)
+        r0 = sy.r.clone()
         torch.cuda.synchronize()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        g = sy.pg.t
 
         def timed(fn, before=None):
             fn()
@@ -322,29 +248,30 @@ def reference_gpu_step(sizes, reps=20):
                 tot += ev[0].elapsed_time(ev[1])
             return tot / reps
 
-        t_begin = timed(lambda: launch("begin_iter", n, [C.c_uint32(n), P(f), P(ef),
-                                                         C.c_float(0.03125), P(rn), P(ps)]))
-        t_idx = timed(lambda: launch("calc_indexes", n, [C.c_uint32(n), C.c_float(aco),
-                                                         C.c_uint32(cps), P(pg["uci"]),
-                                                         P(pg["uoi"]), P(r)]))
-        t_sort = timed(lambda: torch.sort(pg["uci"], stable=True))
-        t_empty = timed(lambda: launch("set_cells_empty", n_c, [C.c_uint32(n_c), P(pg["beg"]),
-                                                                P(pg["end"])]))
-        t_lim = timed(lambda: launch("find_cells_limits", n, [C.c_uint32(n), P(pg["sci"]),
-                                                              P(pg["beg"]), P(pg["end"])]))
-        t_rk1 = timed(lambda: launch("exec_RK_1", n, [C.c_uint32(n), ng, P(ptd), P(r), P(f), P(lr),
-                                                      P(er), P(rn), P(pgd), P(lgd)]))
-        t_rk2 = timed(lambda: launch("exec_RK_2", n, [C.c_uint32(n), ng, P(ptd), P(r), P(f), P(lr),
-                                                      P(er), P(ef), P(rn), P(pgd), P(lgd)]),
-                      before=lambda: r.copy_(r0))
+        t_begin = timed(lambda: mod.launch("begin_iter", n, [
+            C.c_uint32(n), P(sy.f), P(sy.ef), C.c_float(sy.sd), P(sy.rn), P(sy.ps)], stream))
+        t_idx = timed(lambda: mod.launch("calc_indexes", n, [
+            C.c_uint32(n), C.c_float(ref.ACO), C.c_uint32(sy.cps), P(g["uci"]), P(g["uoi"]),
+            P(sy.r)], stream))
+        t_sort = timed(lambda: torch.sort(g["uci"], stable=True))
+        t_empty = timed(lambda: mod.launch("set_cells_empty", sy.pg.n_c, [
+            C.c_uint32(sy.pg.n_c), P(g["beg"]), P(g["end"])], stream))
+        t_lim = timed(lambda: mod.launch("find_cells_limits", n, [
+            C.c_uint32(n), P(g["sci"]), P(g["beg"]), P(g["end"])], stream))
+        t_rk1 = timed(lambda: mod.launch("exec_RK_1", n, [
+            C.c_uint32(n), sy.ng, P(sy.pt), P(sy.r), P(sy.f), P(sy.lr), P(sy.er), P(sy.rn),
+            P(sy.pg.dev), P(sy.lg.dev)], stream))
+        t_rk2 = timed(lambda: mod.launch("exec_RK_2", n, [
+            C.c_uint32(n), sy.ng, P(sy.pt), P(sy.r), P(sy.f), P(sy.lr), P(sy.er), P(sy.ef),
+            P(sy.rn), P(sy.pg.dev), P(sy.lg.dev)], stream), before=lambda: sy.r.copy_(r0))
         step = t_begin + 2 * (t_idx + t_sort + t_empty + t_lim) + t_rk1 + t_rk2
         out.append({"n_beads": int(n), "ms_per_step": step, "bead_steps_per_s": n / (step / 1e3),
                     "ms": {"begin_iter": t_begin, "calc_indexes": t_idx, "sort (CUB via torch)": t_sort,
                            "set_cells_empty": t_empty, "find_cells_limits": t_lim,
                            "exec_RK_1": t_rk1, "exec_RK_2": t_rk2}})
-        if not torch.isfinite(r).all():
+        if not torch.isfinite(sy.r).all():
             raise RuntimeError("non-finite positions in the reference step")
-    ck(cu.cuModuleUnload(mod))
+    mod.close()
     return {"kernels": "ccp's own sm_103a kernels (oracle/_ref/ccp_ref.cubin)",
             "config": "ccp force field, cvf 0.125, laf 0.25 (ccp-profile.cu:55-62), cells of aco = 2",
             "sizes": out}
