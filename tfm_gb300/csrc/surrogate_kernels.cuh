@@ -639,42 +639,50 @@ __global__ void k_pool(const bf16 *__restrict__ h, int L, int C, int f, int n, b
 
 // Pair features of the head input: z0[b][i][j][c] = u_i[c] v_j[c] + u_j[c] v_i[c]
 // + E[|i - j|][c], u = uv[..][0, 64), v = uv[..][64, 128). Block: PAIR_ROWS
-// consecutive rows i of one sample, so each u_j, v_j read serves them all.
+// consecutive rows i0.. of sample b; each warp walks runs of 32 consecutive
+// columns j, lane l holding channels 2l, 2l + 1 (one warp store covers a
+// pixel's 64 channels). A lane keeps u_i, v_i of the block's rows and the
+// distance embedding of every row in registers: the value row r needs at
+// column j + 1, E[|i0 + r - j - 1|], is the one row r - 1 used at column j,
+// so the window shifts by one row per column and only E[|i0 - j - 1|] is
+// loaded. Per pixel and row: u_j, v_j and one E value per PAIR_ROWS outputs.
 constexpr int PAIR_ROWS = 8;
+
+__device__ __forceinline__ float2 ld_bf16x2(const bf16 *p) {
+  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(p));
+}
 
 __global__ void __launch_bounds__(256)
     k_pair_fwd(const bf16 *__restrict__ uv, const float *__restrict__ E, int M, bf16 *__restrict__ z0) {
   const int i0 = blockIdx.x * PAIR_ROWS, b = blockIdx.y;
-  __shared__ __align__(16) float ui[PAIR_ROWS][64], vi[PAIR_ROWS][64];
-  for (int k = threadIdx.x; k < PAIR_ROWS * 64; k += blockDim.x) {
-    const int r = k >> 6, c = k & 63;
-    const bf16 *row = uv + ((size_t)b * M + i0 + r) * 128;
-    ui[r][c] = __bfloat162float(row[c]);
-    vi[r][c] = __bfloat162float(row[64 + c]);
-  }
-  __syncthreads();
-  // thread -> (j, 16-channel chunk) for all PAIR_ROWS rows
-  for (int k = threadIdx.x; k < M * 4; k += blockDim.x) {
-    const int j = k >> 2, c0 = (k & 3) * 16;
-    const bf16 *rj = uv + ((size_t)b * M + j) * 128;
-    float uj[16], vj[16], v[16];
-    load_bf16x16(rj + c0, uj);
-    load_bf16x16(rj + 64 + c0, vj);
-#pragma unroll 2
-    for (int r = 0; r < PAIR_ROWS; ++r) {
-      const int i = i0 + r;
-      const float4 *e4 = reinterpret_cast<const float4 *>(E + (size_t)abs(i - j) * 64 + c0);
-      const float4 *u4 = reinterpret_cast<const float4 *>(&ui[r][c0]);
-      const float4 *w4 = reinterpret_cast<const float4 *>(&vi[r][c0]);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int c = 2 * lane;
+  const bf16 *uvb = uv + (size_t)b * M * 128;
+  const float2 *E2 = reinterpret_cast<const float2 *>(E) + lane;  // E2[d * 32] = E[d][c, c + 1]
+  float2 ui[PAIR_ROWS], vi[PAIR_ROWS];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 e = __ldg(e4 + q), a = u4[q], c = w4[q];
-        v[4 * q] = fmaf(a.x, vj[4 * q], fmaf(uj[4 * q], c.x, e.x));
-        v[4 * q + 1] = fmaf(a.y, vj[4 * q + 1], fmaf(uj[4 * q + 1], c.y, e.y));
-        v[4 * q + 2] = fmaf(a.z, vj[4 * q + 2], fmaf(uj[4 * q + 2], c.z, e.z));
-        v[4 * q + 3] = fmaf(a.w, vj[4 * q + 3], fmaf(uj[4 * q + 3], c.w, e.w));
+  for (int r = 0; r < PAIR_ROWS; ++r) {
+    ui[r] = ld_bf16x2(uvb + (size_t)(i0 + r) * 128 + c);
+    vi[r] = ld_bf16x2(uvb + (size_t)(i0 + r) * 128 + 64 + c);
+  }
+  __nv_bfloat162 *zb = reinterpret_cast<__nv_bfloat162 *>(z0 + (size_t)b * M * M * 64) + lane;
+  for (int j0 = warp * 32; j0 < M; j0 += nw * 32) {
+    float2 e[PAIR_ROWS];
+#pragma unroll
+    for (int r = 0; r < PAIR_ROWS; ++r) e[r] = __ldg(E2 + (size_t)abs(i0 + r - j0) * 32);
+    const int j1 = min(j0 + 32, M);
+    for (int j = j0; j < j1; ++j) {
+      const float2 uj = ld_bf16x2(uvb + (size_t)j * 128 + c);
+      const float2 vj = ld_bf16x2(uvb + (size_t)j * 128 + 64 + c);
+#pragma unroll
+      for (int r = 0; r < PAIR_ROWS; ++r) {
+        const float zx = fmaf(ui[r].x, vj.x, fmaf(uj.x, vi[r].x, e[r].x));
+        const float zy = fmaf(ui[r].y, vj.y, fmaf(uj.y, vi[r].y, e[r].y));
+        zb[((size_t)(i0 + r) * M + j) * 32] = __floats2bfloat162_rn(zx, zy);
       }
-      store_bf16x16(z0 + (((size_t)b * M + i) * M + j) * 64 + c0, v);
+#pragma unroll
+      for (int r = PAIR_ROWS - 1; r > 0; --r) e[r] = e[r - 1];
+      if (j + 1 < j1) e[0] = __ldg(E2 + (size_t)abs(i0 - j - 1) * 32);  // |.| < M
     }
   }
 }
