@@ -567,6 +567,7 @@ SUR_L, SUR_M = 1024, 256
 SUR_FWD_FLOP = (6 * 2 * SUR_M * SUR_M * 9 * 64 * 64 + 2 * SUR_L * 5 * 64 * 128
                 + 7 * 2 * SUR_L * 5 * 128 * 128 + 2 * SUR_M * 128 * 128)
 SIM_STEPS_PER_MAP = 100000  # the batched-ensemble protocol: 1e5 Heun steps per map
+SUR_INFER_BATCH = 128  # sequences per inference batch (training: 32)
 
 
 def bf16_peak():
@@ -644,37 +645,47 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, truth_reps, scr
                                "difference over bin pairs"},
         "simulation_replicas_for_equal_ps_error": reps_equal,
     }
-    # inference throughput, inputs resident: batches of dataset rows
-    st = torch.cuda.ExternalStream(net.stream())
+    # inference: a handle of batch SUR_INFER_BATCH with the trained weights
+    # (training keeps c3's batch of 32; serving takes bigger batches, which
+    # fill the GPU better in the encoder); inputs resident, batches of rows
+    IB = SUR_INFER_BATCH
+    inf = S.Surrogate("batch %d\n" % IB, seed=3)
+    inf.set_params(net.params())
+    inf.set_dataset(types, lad, maps)
+    train_flags = net.error_flags()
+    net.close()
+    st = torch.cuda.ExternalStream(inf.stream())
     rows = np.arange(n_seq, dtype=np.int32)
-    nb = 64
+    nb = max(4, 2048 // IB)
     for i in range(3):
-        net.predict_rows(rows[(i * B) % n_seq:(i * B) % n_seq + B], copy=False)
-    net.synchronize()
+        inf.predict_rows(rows[(i * IB) % (n_seq - IB + 1):][:IB], copy=False)
+    inf.synchronize()
     clocks = Clocks(0)
     clocks.start()
-    k0 = net.kernel_count()
+    k0 = inf.kernel_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
     for i in range(nb):
-        a = (i * B) % (n_seq - B + 1)
-        net.predict_rows(rows[a:a + B], copy=False)
+        a = (i * IB) % (n_seq - IB + 1)
+        inf.predict_rows(rows[a:a + IB], copy=False)
     e1.record(st)
-    net.synchronize()
+    inf.synchronize()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    maps_s = nb * B / (ms / 1000.0)
+    maps_s = nb * IB / (ms / 1000.0)
     peak, kind = bf16_peak()
     tflops = maps_s * SUR_FWD_FLOP / 1e12
     sim_maps_s = bead_steps_per_s / (SUR_L * SIM_STEPS_PER_MAP)
     # end to end: host sequences in, host maps out
-    tt, tl = types[:256], lad[:256]
-    net.predict(tt[:B], tl[:B])
+    tt, tl = types[:512], lad[:512]
+    inf.predict(tt[:IB], tl[:IB])
     t2 = time.perf_counter()
-    net.predict(tt, tl)
-    e2e = 256 / (time.perf_counter() - t2)
+    inf.predict(tt, tl)
+    e2e = 512 / (time.perf_counter() - t2)
+    net = inf  # screening below runs on the inference handle
     rep.update({
-        "maps_per_s": maps_s, "ms_per_batch_of_32": ms / nb, "gpu_launches_per_batch": (net.kernel_count() - k0) / nb,
+        "maps_per_s": maps_s, "inference_batch": IB, "ms_per_batch": ms / nb,
+        "gpu_launches_per_batch": (inf.kernel_count() - k0) / nb,
         "clocks": clk,
         "roofline": {"bound": "tensor", "kernel": "forward pass (head 3x3 convolutions dominate)",
                      "achieved": tflops, "peak": peak, "peak_kind": kind, "unit": "TFLOP/s",
@@ -695,7 +706,7 @@ def surrogate_report(bead_steps_per_s, n_seq, sim_steps, epochs, truth_reps, scr
         srep, _ = S.screen(net, stypes, slad, env, 0.01, seed=11, sim=sim)
         rep["screening"] = dict(srep, workload="c4: %d new seeded sequences, 1%% random + "
                                                "out-of-envelope re-simulated" % screen_n)
-    rep["error_flags"] = net.error_flags()
+    rep["error_flags"] = train_flags | net.error_flags()
     net.close()
     return rep
 
