@@ -91,10 +91,12 @@ struct ConvEpi {
 // shared memory after the operand tiles: barriers (256 B), TMEM slot and
 // abort flag (256 B), bias [128], output weights [64]
 constexpr uint32_t CONV_SMEM_TAIL = 256u + 256u + 512u + 256u;
+// then one 2 KB staging tile per epilogue warp (32 pixels x 32 BF16 channels)
+constexpr uint32_t EPI_STAGE_BYTES = 32u * 32u * 2u;
 
 __host__ __device__ constexpr uint32_t conv_smem_bytes(int ntaps, int cin_blocks, int N, int stages) {
   return 1024u + (uint32_t)(ntaps * cin_blocks) * (uint32_t)N * 128u + (uint32_t)stages * WIN_BYTES +
-         CONV_SMEM_TAIL;
+         CONV_SMEM_TAIL + (uint32_t)EPI_WARPS * EPI_STAGE_BYTES;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -163,12 +165,40 @@ __device__ __forceinline__ void conv_epilogue_load(const ConvEpi &e, size_t p, i
   ld.rdy = e.resid_dy ? e.resid_dy[p] : 0.0f;
 }
 
+// Stores the 32 BF16 channels v of this lane's pixel (pixel pbase + lane,
+// channels c0 ..) for the whole warp: the 32 x 64 B are staged in the warp's
+// shared-memory tile (16-byte chunks XOR-swizzled by pixel, so neither the
+// lane-per-pixel writes nor the pixel-pair reads conflict on banks), then
+// each store instruction writes 8 pixels' 64 contiguous bytes. Written
+// directly, every 16-byte store would touch 32 different lines.
+template <int N>
+__device__ __forceinline__ void store_row_bf16x32(bf16 *out, size_t pbase, int c0, const float *v,
+                                                  uint4 *stage) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    stage[lane * 4 + (k ^ ((lane >> 1) & 3))] =
+        make_uint4(pack_bf16(v[8 * k], v[8 * k + 1]), pack_bf16(v[8 * k + 2], v[8 * k + 3]),
+                   pack_bf16(v[8 * k + 4], v[8 * k + 5]), pack_bf16(v[8 * k + 6], v[8 * k + 7]));
+  __syncwarp();
+  const int c = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int pr = (lane >> 2) + 8 * i;
+    reinterpret_cast<uint4 *>(out + (pbase + (size_t)pr) * N + c0)[c] =
+        stage[pr * 4 + (c ^ ((pr >> 1) & 3))];
+  }
+  __syncwarp();
+}
+
 // Epilogue of one output pixel p for the thread's half of the N channels
-// (32 N / 64 columns from TMEM address taddr), with its global inputs in ld.
+// (32 N / 64 columns from TMEM address taddr), with its global inputs in ld;
+// stage: the warp's 2 KB staging tile for the BF16 output.
 // Returns this thread's partial output-layer dot (0 without wo).
 template <int N>
 __device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float *sbias, const float *swo,
-                                                   size_t p, int half, uint32_t taddr, const EpiLoads<N> &ld) {
+                                                   size_t p, int half, uint32_t taddr, const EpiLoads<N> &ld,
+                                                   uint4 *stage) {
   constexpr int G = N / 64;
   const int c_begin = half * (N / 2);
   const float rdy = ld.rdy;
@@ -230,10 +260,7 @@ __device__ __forceinline__ float conv_epilogue_row(const ConvEpi &e, const float
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = ((ld.mi[g] >> i) & 1u) ? v[i] : 0.0f;
     }
-    if (e.out) {
-      store_bf16x16(e.out + o, v);
-      store_bf16x16(e.out + o + 16, v + 16);
-    }
+    if (e.out) store_row_bf16x32<N>(e.out, p - (size_t)(threadIdx.x & 31), c0, v, stage);
   }
   return dot;
 }
@@ -265,6 +292,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
   volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
   float *sbias = reinterpret_cast<float *>(tail + 256);
   float *swo = sbias + 128;  // [64]
+  uint4 *epi_stage = reinterpret_cast<uint4 *>(smem_raw + (bar0 + CONV_SMEM_TAIL - raw));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -401,7 +429,8 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       if (!tc::mbar_wait(tfull0 + 8u * buf, use & 1u, abort)) break;
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N);
-      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr, ld);
+      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr, ld,
+                                             epi_stage + (warp - 1 - MMA_WARPS) * (EPI_STAGE_BYTES / 16));
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tempty0 + 8u * buf);
