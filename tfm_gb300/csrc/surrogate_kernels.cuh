@@ -143,18 +143,37 @@ struct EpiLoads {
   float rdy;
 };
 
+// The 32 BF16 channels (c0 ..) of this lane's pixel pbase + lane, loaded for
+// the whole warp: each load instruction reads 8 pixels' 64 contiguous bytes
+// into the warp's staging tile (the swizzle of store_row_bf16x32), from
+// which every lane takes its own pixel's 64 bytes.
 template <int N>
-__device__ __forceinline__ void conv_epilogue_load(const ConvEpi &e, size_t p, int half, EpiLoads<N> &ld) {
+__device__ __forceinline__ void load_row_bf16x32(const bf16 *src, size_t pbase, int c0, uint4 *dst,
+                                                 uint4 *stage) {
+  const int lane = threadIdx.x & 31;
+  const int c = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int pr = (lane >> 2) + 8 * i;
+    stage[pr * 4 + (c ^ ((pr >> 1) & 3))] =
+        reinterpret_cast<const uint4 *>(src + (pbase + (size_t)pr) * N + c0)[c];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) dst[k] = stage[lane * 4 + (k ^ ((lane >> 1) & 3))];
+  __syncwarp();
+}
+
+template <int N>
+__device__ __forceinline__ void conv_epilogue_load(const ConvEpi &e, size_t p, int half, EpiLoads<N> &ld,
+                                                   uint4 *stage) {
   constexpr int G = N / 64;  // 32-column groups per thread
   const int c_begin = half * (N / 2);
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const size_t o = p * (size_t)N + c_begin + 32 * g;
-    if (e.resid) {
-      const uint4 *s = reinterpret_cast<const uint4 *>(e.resid + o);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) ld.rb[g][i] = s[i];
-    }
+    if (e.resid)
+      load_row_bf16x32<N>(e.resid, p - (size_t)(threadIdx.x & 31), c_begin + 32 * g, ld.rb[g], stage);
     if (e.resid_f32) {
       const float4 *s = reinterpret_cast<const float4 *>(e.resid_f32 + o);
 #pragma unroll
@@ -425,12 +444,12 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       const int wb = tile % wtiles, bh = tile / wtiles;
       const size_t p = (size_t)bh * sh.W + (size_t)wb * 128 + row;
       EpiLoads<N> ld;
-      conv_epilogue_load<N>(epi, p, half, ld);  // before the accumulator is ready
+      uint4 *stage = epi_stage + (warp - 1 - MMA_WARPS) * (EPI_STAGE_BYTES / 16);
+      conv_epilogue_load<N>(epi, p, half, ld, stage);  // before the accumulator is ready
       if (!tc::mbar_wait(tfull0 + 8u * buf, use & 1u, abort)) break;
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N);
-      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr, ld,
-                                             epi_stage + (warp - 1 - MMA_WARPS) * (EPI_STAGE_BYTES / 16));
+      const float dot = conv_epilogue_row<N>(epi, sbias, swo, p, half, taddr, ld, stage);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tempty0 + 8u * buf);
