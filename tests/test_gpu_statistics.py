@@ -18,8 +18,10 @@ oracle): per replica the marginal-standard-error thermalisation and the
 blocking standard error, then the inverse-variance combination over
 replicas. Each observable must satisfy |mean_ref - mean_engine| <=
 3 sqrt(sem_ref^2 + sem_engine^2). Because a replica's two runs share their
-start, the difference per replica is also tested directly (paired, 4 standard
-errors over the replicas: the start's contribution cancels there).
+start, the difference per replica is also tested directly (paired: the
+start's contribution cancels there). Its bound is 5 standard errors over the
+16 replicas: with 15 degrees of freedom and 18 observables a bound of 4 would
+fail by chance in ~2 % of runs, one of 5 in ~0.3 %.
 """
 import math
 
@@ -151,5 +153,5 @@ def test_engine_samples_what_ccp_samples(engine_lib):
         print("%-34s %.6g +- %.2g | %.6g +- %.2g | %.2f | %.2f" % (name, mr, er, me, ee, z, zp))
         worst = max(worst, z)
         assert z <= 3.0, (name, mr, er, me, ee)
-        assert zp <= 4.0, (name, md, ed)
+        assert zp <= 5.0, (name, md, ed)
     print("largest |difference| / combined sem: %.2f" % worst)
