@@ -88,7 +88,9 @@ typedef int (*ccpgpu_frame_fn)(void *user, uint32_t frame_index, float time,
 int ccpgpu_create(const char *param_text, uint64_t seed, ccpgpu_sim **out);
 
 /* Batch of n_systems independent systems sharing the force field and keys of
- * param_text. n_beads[i] >= 1 beads in n_chains[i] equal chains (NULL: 1 chain),
+ * param_text. n_beads[i] >= 1 beads in n_chains[i] equal chains (NULL: the
+ * number_of_chains key, else 1 chain; ccp's 30386-bead model defaults to, and
+ * with 12 chains uses, its 12 chromosomes of chrdat.cuh:28-31, as ccpgpu_create does),
  * nucleus radius radii[i] (NULL: from the packing fraction or the
  * nucleus_radius key) and Philox seed seeds[i] (NULL: seed + i). No reference
  * counterpart: ccp runs replicas as separate processes (Scripts/makeallsim.py:105-121). */

@@ -40,6 +40,10 @@ NAMES = {
                  "S6_PNS_6sugridES8_",
     "exec_RK_2": "_ZN3mmc9exec_RK_2ILNS_5stypeE0EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_S6_"
                  "S6_S6_PNS_6sugridES8_",
+    "exec_RK_1_icg": "_ZN3mmc9exec_RK_1ILNS_5stypeE1EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_"
+                     "S6_S6_PNS_6sugridES8_",
+    "exec_RK_2_icg": "_ZN3mmc9exec_RK_2ILNS_5stypeE1EEEvjNS_6cngeomEPNS_5ptypeEPNS_5vec3fES6_S6_"
+                     "S6_S6_S6_PNS_6sugridES8_",
 }
 
 
@@ -177,19 +181,23 @@ class System:
             mod.launch("init_ps", n, [C.c_uint32(n), _p(self.ps), C.c_uint32(seed)], stream)
             self.lg.build(self.lr)  # built once per run (chrsim.cu:561)
 
-    def step(self):
-        """One stochastic Heun step (chrsim.cu:572-580)."""
+    def step(self, icg=False):
+        """One stochastic Heun step (chrsim.cu:572-580); icg: one step of the
+        initial-condition relaxation instead (soft repulsion, no noise,
+        chrsim.cu:500-509)."""
         m, n, s = self.mod, self.n, self.stream
-        m.launch("begin_iter", n, [C.c_uint32(n), _p(self.f), _p(self.ef), C.c_float(self.sd),
-                                   _p(self.rn), _p(self.ps)], s)
+        sfx = "_icg" if icg else ""
+        m.launch("begin_iter", n, [C.c_uint32(n), _p(self.f), _p(self.ef),
+                                   C.c_float(0.0 if icg else self.sd), _p(self.rn), _p(self.ps)],
+                 s)
         self.pg.build(self.r)
-        m.launch("exec_RK_1", n, [C.c_uint32(n), self.ng, _p(self.pt), _p(self.r), _p(self.f),
-                                  _p(self.lr), _p(self.er), _p(self.rn), _p(self.pg.dev),
-                                  _p(self.lg.dev)], s)
+        m.launch("exec_RK_1" + sfx, n, [C.c_uint32(n), self.ng, _p(self.pt), _p(self.r),
+                                        _p(self.f), _p(self.lr), _p(self.er), _p(self.rn),
+                                        _p(self.pg.dev), _p(self.lg.dev)], s)
         self.pg.build(self.er)
-        m.launch("exec_RK_2", n, [C.c_uint32(n), self.ng, _p(self.pt), _p(self.r), _p(self.f),
-                                  _p(self.lr), _p(self.er), _p(self.ef), _p(self.rn),
-                                  _p(self.pg.dev), _p(self.lg.dev)], s)
+        m.launch("exec_RK_2" + sfx, n, [C.c_uint32(n), self.ng, _p(self.pt), _p(self.r),
+                                        _p(self.f), _p(self.lr), _p(self.er), _p(self.ef),
+                                        _p(self.rn), _p(self.pg.dev), _p(self.lg.dev)], s)
 
     def max_radius(self):
         return float(self.r.norm(dim=1).max())

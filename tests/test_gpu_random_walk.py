@@ -120,3 +120,45 @@ def test_stuck_walk_ends_with_error(engine_lib):
     ok = ChrSim(ccp_params(2048)[0], seed=4)
     ok.generate_initial_condition()
     assert ok.overlaps().sum() == 0
+
+
+@pytest.mark.gpu
+def test_diploid_batch_walks_like_single_systems(engine_lib, orc):
+    """A batch of ccp's 30386-bead model defaults to its 12 chromosomes at
+    ccp's limits, like a single system created from the same text: each
+    system's walk equals that system's walk alone."""
+    from tfm_gb300.ccpgpu import Batch, ChrSim
+
+    txt, R, n_l = ccp_params(orc.N_DEF)
+    bt = Batch(txt, [orc.N_DEF] * 2, seeds=[5, 6])
+    assert [bt.system_info(s).n_chains for s in range(2)] == [12, 12]
+    draws = bt.random_walk()
+    xb = bt.positions()
+    one = ChrSim(txt, seed=6)
+    d1 = one.random_walk()
+    assert np.array_equal(d1, draws[12:])
+    o = bt.system_info(1).bead_offset
+    assert np.array_equal(one.positions(), xb[o:o + orc.N_DEF])
+
+
+@pytest.mark.gpu
+def test_large_ccp_relaxation_stays_confined(engine_lib):
+    """Relaxing 16 walks of 30385 beads in ccp's force field ends with no
+    overlapping pair and every bead inside its nucleus. Without the cap on a
+    relaxation stage's displacement, beads pushed close to the wall got a
+    Wang-Frenkel wall force that threw them out of the nucleus (positions up
+    to 1e17) in 10 of these 16 systems."""
+    from tfm_gb300.ccpgpu import Batch
+
+    n, m = 30385, 16
+    txt, R, n_l = ccp_params(n)
+    bt = Batch(txt, [n] * m, seeds=np.arange(m, dtype=np.uint64) + 101)
+    bt.generate_initial_condition()
+    flags, _ = bt.error_flags()
+    assert not flags[:4].any(), flags
+    assert int(bt.overlaps().sum()) == 0
+    x = bt.positions()
+    for s in range(m):
+        si = bt.system_info(s)
+        r = np.linalg.norm(x[si.bead_offset:si.bead_offset + si.n_beads], axis=1)
+        assert r.max() < si.nucleus_radius, s

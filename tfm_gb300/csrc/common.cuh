@@ -59,6 +59,7 @@ struct ForceField {
   float dt;         // time step
   float sd;         // noise standard deviation sqrt(2 kT dt)
   float kT;         // thermal energy
+  float icg_max_step;  // the same cap for the relaxation steps (MODE_ICG)
 };
 
 // ---------------------------------------------------------------- systems

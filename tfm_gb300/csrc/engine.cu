@@ -1510,8 +1510,18 @@ int ccpgpu_batch_create(const char *param_text, int32_t n_systems, const int32_t
       SystemSpec &q = sp[s];
       q.n = n_beads[s];
       need(q.n >= 1, "system without beads");
-      q.n_chains = n_chains ? n_chains[s] : 1;
+      const bool diploid_size = p.preset == PRESET_CCP && (uint32_t)q.n == CCP_N_DEF;
+      if (n_chains)
+        q.n_chains = n_chains[s];
+      else if (pm.has("number_of_chains"))
+        q.n_chains = p.n_chains;
+      else
+        q.n_chains = diploid_size ? 12 : 1;
       need(q.n_chains >= 1 && q.n_chains <= q.n, "bad chain count");
+      // ccp's diploid model: 12 chromosomes at its fixed limits (chrdat.cuh:28-31),
+      // as a single system created from the same text
+      if (diploid_size && q.n_chains == 12)
+        for (int c = 0; c < 12; ++c) q.chain_first.push_back((int)CCP_CHR_LIM[c]);
       if (radii)
         q.R_n = radii[s];
       else if (pm.has("nucleus_radius"))

@@ -85,6 +85,14 @@ static ForceField preset_ccp(float T) {
   f.rc_icg = CCP_RCO;
   f.mis = CCP_MIS;
   f.max_step = 0.0f;
+  // ccp's relaxation has no cap either (chrsim.cu:500-509), but there a bead
+  // pushed within ~0.35 sigma of the wall by overlapping neighbours gets a
+  // Wang-Frenkel wall force (~96 / gap^7) that moves it hundreds of sigma in
+  // one step, out of the nucleus; 16 relaxations of 30385-bead walks never
+  // finished without one. The soft repulsion alone moves a bead < 0.07 sigma
+  // per overlapping neighbour and stage, so a 0.25 sigma cap leaves ordinary
+  // relaxation steps as they are.
+  f.icg_max_step = 0.25f;
   f.dt = (float)CCP_DT;
   f.kT = CCP_K_B * T;
   f.sd = (float)std::sqrt(2.0 * CCP_K_B * T * CCP_DT);  // chrsim.cu:424
@@ -115,6 +123,7 @@ static ForceField preset_baseline(float kT, float dt) {
   // a 5-sigma noise jump can bring a WCA pair to r ~ 0.7, where one corrector
   // step would move it several sigma: cap the deterministic displacement
   f.max_step = 0.1f;
+  f.icg_max_step = f.max_step;
   f.dt = dt;
   f.kT = kT;
   f.sd = (float)std::sqrt(2.0 * (double)kT * (double)dt);

@@ -1265,7 +1265,7 @@ __global__ void __launch_bounds__(256, 7)
   float4 out;
   if (STAGE == 1) {
     float3 D = make_float3(F.x * ff.dt, F.y * ff.dt, F.z * ff.dt);
-    cap_step(D, ff.max_step);
+    cap_step(D, MODE == MODE_ICG ? ff.icg_max_step : ff.max_step);
     out = make_float4(xi.x + D.x + rn.x, xi.y + D.y + rn.y, xi.z + D.z + rn.z, xi.w);
     er[i] = out;
     fbuf[i] = make_float4(F.x, F.y, F.z, 0.0f);
@@ -1274,7 +1274,7 @@ __global__ void __launch_bounds__(256, 7)
     float4 f1 = fbuf[i];
     float h = 0.5f * ff.dt;
     float3 D = make_float3((f1.x + F.x) * h, (f1.y + F.y) * h, (f1.z + F.z) * h);
-    cap_step(D, ff.max_step);
+    cap_step(D, MODE == MODE_ICG ? ff.icg_max_step : ff.max_step);
     out = make_float4(r.x + D.x + rn.x, r.y + D.y + rn.y, r.z + D.z + rn.z, r.w);
     pos[i] = out;
   }

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS, 1)
       const float3 rn = persist_noise<MODE>(i, st, s, ff, err);
       m.f1[i] = F;
       float3 D = make_float3(F.x * ff.dt, F.y * ff.dt, F.z * ff.dt);
-      cap_step(D, ff.max_step);
+      cap_step(D, MODE == MODE_ICG ? ff.icg_max_step : ff.max_step);
       const float4 e = make_float4(x.x + D.x + rn.x, x.y + D.y + rn.y, x.z + D.z + rn.z, x.w);
       m.fs[k] = make_float3(e.x, e.y, e.z);  // this slot's pair force is consumed
       if (!(isfinite(e.x) && isfinite(e.y) && isfinite(e.z))) set_err(err, ERR_NAN);
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS, 1)
       const float4 x = m.r[i];
       const float3 f1 = m.f1[i];
       float3 D = make_float3((f1.x + F.x) * h, (f1.y + F.y) * h, (f1.z + F.z) * h);
-      cap_step(D, ff.max_step);
+      cap_step(D, MODE == MODE_ICG ? ff.icg_max_step : ff.max_step);
       const float4 o = make_float4(x.x + D.x + rn.x, x.y + D.y + rn.y, x.z + D.z + rn.z, x.w);
       if (!(isfinite(o.x) && isfinite(o.y) && isfinite(o.z))) set_err(err, ERR_NAN);
       m.rank[i] = (uint16_t)atomicAdd(&m.cell[persist_cell(o, g, err)], 1u);

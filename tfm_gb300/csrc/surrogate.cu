@@ -178,7 +178,8 @@ struct Launcher {
     if (std::abs(sh.step_w) * (C / 2) > WIN_RADIUS) throw Error(ST_ARG, "tap column offset above the window radius");
     const int cb = cin / 64;
     sh.stages = MAX_STAGES;
-    while (sh.stages > 2 && (int)conv_smem_bytes(nt, cb, N, sh.stages) > d.max_smem) --sh.stages;
+    while (sh.stages > MMA_WARPS && (int)conv_smem_bytes(nt, cb, N, sh.stages) > d.max_smem)
+      sh.stages -= MMA_WARPS;
     const uint32_t smem = conv_smem_bytes(nt, cb, N, sh.stages);
     if ((int)smem > d.max_smem) throw Error(ST_ARG, "convolution weights do not fit in shared memory");
     sh.n_tiles = B * H * (W / 128);
@@ -757,7 +758,11 @@ struct Net {
     SCK(cudaStreamSynchronize(st));
     if (flags) {
       err.zero(st);
-      throw Error(ST_STATE, "a tensor-core kernel gave up waiting for its pipeline");
+      throw Error(ST_STATE, std::string("a tensor-core kernel (") +
+                                ((flags & 1) ? "convolution" : "") +
+                                ((flags & 3) == 3 ? ", " : "") +
+                                ((flags & 2) ? "weight gradient" : "") +
+                                ") gave up waiting for its pipeline");
     }
   }
 

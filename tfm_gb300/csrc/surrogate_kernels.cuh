@@ -37,8 +37,8 @@ namespace sur {
 using bf16 = __nv_bfloat16;
 
 constexpr int MAX_TAPS = 9;
-// warp 0: TMA; warps 1-2: MMA issue, alternate tiles (warp 1 also owns
-// TMEM); warps 3-10: epilogue (two warps per TMEM lane quarter, each taking
+// warp 0: TMA; warps 1-2: MMA issue, alternate tiles, each from its own ring
+// of input windows (warp 1 also owns TMEM); warps 3-10: epilogue (two warps per TMEM lane quarter, each taking
 // half of the output channels). Two issuing warps keep the tensor core fed:
 // one thread issues a 128 x N x 16 MMA every ~90 cycles, the tensor core
 // runs a 128 x 64 x 16 MMA every 48.
@@ -46,6 +46,7 @@ constexpr int MMA_WARPS = 2;
 constexpr int CONV_THREADS = 32 * (1 + MMA_WARPS + 8);
 constexpr int EPI_WARPS = 8;
 constexpr int MAX_STAGES = 8;
+static_assert(MAX_STAGES % MMA_WARPS == 0, "window rings of equal size");
 constexpr uint32_t TMEM_COLS_CONV = 256;  // 256 / N accumulators of N columns
 
 // A-operand windows: the input pixels [w0 - WIN_RADIUS, w0 + 128 + WIN_RADIUS)
@@ -63,7 +64,7 @@ constexpr uint32_t WIN_BYTES = (uint32_t)WIN_ROWS * 128u;  // a multiple of 1024
 // input-gradient convolution); |dw| <= WIN_RADIUS.
 struct ConvShape {
   int B, H, W;     // image (input = output size); W is a multiple of 128
-  int stages;      // A-window pipeline depth (2..MAX_STAGES)
+  int stages;      // A-window slots (a multiple of MMA_WARPS, up to MAX_STAGES)
   int n_tiles;     // B * H * W / 128
   int step_h, step_w;
 };
@@ -296,7 +297,12 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
   const uint32_t raw = tc::smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   constexpr int nwt = R * C * CB;  // resident weight tiles
+  // A windows: S slots, S / MMA_WARPS in each MMA warp's own ring. The warps
+  // take alternate tiles; with one shared ring a warp would skip the other's
+  // windows and could wait on a slot's barrier a whole phase ahead of the
+  // last one it saw, where a parity wait passes on the stale phase.
   const int S = sh.stages;
+  const int Sm = S / MMA_WARPS;
   const uint32_t w_tile = (uint32_t)N * 128u;
   const uint32_t w_base = base;
   const uint32_t a_base = w_base + (uint32_t)nwt * w_tile;
@@ -346,36 +352,33 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
       for (int t = 0; t < R * C; ++t)
         for (int cb = 0; cb < CB; ++cb)
           tc::tma_load_2d(w_base + (uint32_t)(t * CB + cb) * w_tile, &tmw, wbar, cb * 64, t * N);
-      int s = 0;
-      uint32_t ph = 0;
-      uint32_t issued = 0;
-      for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x) {
+      // windows issued so far to each MMA warp's ring
+      uint32_t issued[MMA_WARPS] = {};
+      int local = 0;
+      for (int tile = blockIdx.x; tile < sh.n_tiles; tile += gridDim.x, ++local) {
+        const int m = local % MMA_WARPS;
         const int wb = tile % wtiles, bh = tile / wtiles;
         const int h = bh % sh.H, b = bh / sh.H;
         for (int r = 0; r < R; ++r)
           for (int cb = 0; cb < CB; ++cb) {
-            if (!tc::mbar_wait(empty0 + 8u * s, ph ^ 1u, abort)) goto produced;
-            tc::mbar_arrive_expect_tx(full0 + 8u * s, WIN_BYTES);
-            tc::tma_load_4d(a_base + (uint32_t)s * WIN_BYTES, &tmx, full0 + 8u * s, cb * 64,
+            const uint32_t n = issued[m];
+            const uint32_t slot = (uint32_t)(m * Sm) + n % (uint32_t)Sm;
+            const uint32_t ph = (n / (uint32_t)Sm) & 1u;
+            if (!tc::mbar_wait(empty0 + 8u * slot, ph ^ 1u, abort)) goto produced;
+            tc::mbar_arrive_expect_tx(full0 + 8u * slot, WIN_BYTES);
+            tc::tma_load_4d(a_base + slot * WIN_BYTES, &tmx, full0 + 8u * slot, cb * 64,
                             wb * 128 - WIN_RADIUS, h + (r - R / 2) * sh.step_h, b);
-            ++issued;
-            if (++s == S) {
-              s = 0;
-              ph ^= 1u;
-            }
+            issued[m] = n + 1u;
           }
       }
     produced:
       // nothing may still be landing in shared memory when the CTA exits:
-      // wait for the last (up to S) windows issued, newest first
+      // wait for the last (up to Sm) windows issued to each ring
       tc::mbar_drain(wbar, 0);
-      for (uint32_t k = 0; k < issued && k < (uint32_t)S; ++k) {
-        if (--s < 0) {
-          s = S - 1;
-          ph ^= 1u;
-        }
-        tc::mbar_drain(full0 + 8u * s, ph);
-      }
+      for (int m = 0; m < MMA_WARPS; ++m)
+        for (uint32_t n = issued[m] - min(issued[m], (uint32_t)Sm); n < issued[m]; ++n)
+          tc::mbar_drain(full0 + 8u * ((uint32_t)(m * Sm) + n % (uint32_t)Sm),
+                         (n / (uint32_t)Sm) & 1u);
     }
   } else if (warp <= MMA_WARPS) {
     if (lane == 0) {
@@ -393,9 +396,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
           const int buf = local % ACC;
           if (!tc::mbar_wait(tempty0 + 8u * buf, (((uint32_t)(local / ACC)) & 1u) ^ 1u, abort)) break;
           tc::fence_after_sync();
-          // this tile's windows: global window indices local * KB ...
-          int s = (int)(((uint32_t)local * KB) % (uint32_t)S);
-          uint32_t ph = (((uint32_t)local * KB) / (uint32_t)S) & 1u;
+          // this tile's windows: indices (local / MMA_WARPS) * KB ... of this
+          // warp's own ring
+          const uint32_t n0 = (uint32_t)(local / MMA_WARPS) * KB;
+          int s = (int)(n0 % (uint32_t)Sm);
+          uint32_t ph = (n0 / (uint32_t)Sm) & 1u;
           const uint32_t d = tmem + (uint32_t)(buf * N);
           uint32_t acc = 0;
           bool ok = true;
@@ -403,12 +408,13 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
           for (int r = 0; r < R && ok; ++r)
 #pragma unroll
             for (int cb = 0; cb < CB; ++cb) {
-              if (!tc::mbar_wait(full0 + 8u * s, ph, abort)) {
+              const uint32_t slot = (uint32_t)(m * Sm + s);
+              if (!tc::mbar_wait(full0 + 8u * slot, ph, abort)) {
                 ok = false;
                 break;
               }
               tc::fence_after_sync();
-              const uint32_t win = a_base + (uint32_t)s * WIN_BYTES;
+              const uint32_t win = a_base + slot * WIN_BYTES;
 #pragma unroll
               for (int c = 0; c < C; ++c) {
                 const uint32_t a0 = win + (uint32_t)(WIN_RADIUS + (c - C / 2) * sh.step_w) * 128u;
@@ -419,8 +425,8 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
                   acc = 1;
                 }
               }
-              tc::mma_commit(empty0 + 8u * s);
-              if (++s == S) {
+              tc::mma_commit(empty0 + 8u * slot);
+              if (++s == Sm) {
                 s = 0;
                 ph ^= 1u;
               }
