@@ -283,7 +283,7 @@ int ccpgpu_contact_map_bin(ccpgpu_sim *h, char *buf, size_t cap, size_t *len);
  * system without lamina-binding sites (chain heads every n_beads / n_chains
  * beads, the preset's default force field and cell grid).
  *
- * Scratch: a static device array of about 3.4 MB inside the library, held by
+ * Scratch: a static device array of about 2.9 MB inside the library, held by
  * every GPU that loads it until the process exits. Limits: n_beads <=
  * CCPGPU_NOALLOC_MAX_BEADS and cells_per_side^3 <= CCPGPU_NOALLOC_MAX_CELLS;
  * larger systems are rejected with CCPGPU_ERR_ARG. The first call on a device

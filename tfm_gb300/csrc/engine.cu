@@ -2044,7 +2044,7 @@ constexpr size_t OFF_FS = OFF_SORTED + al(sizeof(float4) * (MAX_BEADS + 1));
 constexpr size_t OFF_FOUT = OFF_FS + al(sizeof(float4) * (MAX_BEADS + 1));
 constexpr size_t OFF_RANK = OFF_FOUT + al(sizeof(float4) * (MAX_BEADS + 1));
 constexpr size_t OFF_COUNTS = OFF_RANK + al(sizeof(uint32_t) * (MAX_BEADS + 1));
-constexpr size_t OFF_START = OFF_COUNTS + al(sizeof(uint32_t) * SCAN_CELLS);
+constexpr size_t OFF_START = OFF_COUNTS + al(SCAN_CELLS);  // one byte count per cell
 constexpr size_t OFF_BSUM = OFF_START + al(sizeof(uint32_t) * (SCAN_CELLS + 4));
 constexpr size_t OFF_TILES = OFF_BSUM + al(sizeof(uint32_t) * (SCAN_BLOCKS + 1));
 constexpr size_t OFF_SYS = OFF_TILES + al(sizeof(Tile) * MAX_TILES);
@@ -2052,7 +2052,7 @@ constexpr size_t OFF_STEP = OFF_SYS + al(sizeof(SysDesc));
 constexpr size_t OFF_ERR = OFF_STEP + al(sizeof(unsigned long long));
 constexpr size_t BYTES = OFF_ERR + al(sizeof(int) * ERR_COUNT);
 
-// The scratch: about 3.4 MB, held by every GPU that loads the library until
+// The scratch: about 2.9 MB, held by every GPU that loads the library until
 // the process exits. Device code could name it directly; host code only knows
 // its host-side stand-in and obtains the device address per device below.
 static __device__ __align__(256) unsigned char scratch[BYTES];
@@ -2176,7 +2176,7 @@ extern "C" int ccpgpu_forces_noalloc(const ccpgpu_noalloc_system *sysp, const fl
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // the array keeps the previous call's contents: clear what must start at zero
-    CK(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (size_t)nblk * SCAN_CHUNK, s));
+    CK(cudaMemsetAsync(counts, 0, (size_t)nblk * SCAN_CHUNK, s));  // byte counts
     CK(cudaMemsetAsync(err, 0, sizeof(int) * ERR_COUNT, s));
     k_na_setup<<<(n_tiles + 127) / 128, 128, 0, s>>>(d, tiles, sys, n_tiles);
     k_na_pack<<<(a.n_beads + 1 + 255) / 256, 256, 0, s>>>(
