@@ -154,6 +154,10 @@ CONV_CASES = [
     (2, 1, 256, 64, 128, "enc5", True, False),
     (2, 1, 256, 128, 128, "one", False, False),
     (2, 3, 256, 64, 64, "head1neg", False, False),
+    # several tiles per CTA: both MMA-issuing warps, their window rings and
+    # the TMEM accumulators wrap around
+    (4, 128, 256, 64, 64, "head2", True, True),
+    (8, 64, 256, 128, 128, "enc5", True, False),
 ]
 
 
@@ -186,9 +190,12 @@ def test_conv_layer_matches_oracle(engine_lib, case):
     got = surrogate.from_bf16(out).astype(np.float64)
     ref_b = surrogate.from_bf16(surrogate.to_bf16(ref.astype(np.float32))).astype(np.float64)
     err = np.abs(got - ref_b)
-    # one BF16 step of the value: 2^(floor(log2 |ref|) - 7)
+    # one BF16 step of the value: 2^(floor(log2 |ref|) - 7), plus 2e-5 for
+    # outputs near zero that cancel (a sum of O(1) terms, or a pre-activation
+    # of ~1.5 against an equal residual), where the FP32 sum's own rounding
+    # (~1e-6) exceeds the step
     ulp = 2.0 ** (np.floor(np.log2(np.maximum(np.abs(ref), 1e-30))) - 7)
-    assert np.all(err <= ulp + 1e-6), (err.max(), np.argmax(err - ulp))
+    assert np.all(err <= ulp + 2e-5), (err.max(), np.argmax(err - ulp))
     assert np.count_nonzero(err) <= 0.01 * err.size
     # mask bits: pre-activation > 0, except where the FP32 and FP64 sums straddle 0
     bits = np.unpackbits(mask.view(np.uint8), bitorder="little").reshape(B, H, W, cout)
@@ -204,6 +211,7 @@ def test_conv_layer_matches_oracle(engine_lib, case):
     (2, 1, 256, 64, 128, "enc5"),
     (2, 1, 256, 128, 128, "one"),
     (1, 5, 128, 64, 64, "head8"),
+    (4, 64, 256, 64, 64, "head2"),
 ])
 def test_wgrad_layer_matches_oracle(engine_lib, case):
     from oracle import surrogate_oracle as so
