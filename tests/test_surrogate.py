@@ -285,6 +285,29 @@ def test_network_forward_matches_oracle(engine_lib):
 
 
 @pytest.mark.gpu
+def test_full_size_forward_matches_oracle(engine_lib):
+    """The default network (1024 beads, 256 bins, 8 encoder and 6 head
+    layers) on two sequences: every convolution runs over several tiles per
+    CTA, as in training and screening, and the maps equal the oracle's."""
+    from oracle import surrogate_oracle as so
+    from tfm_gb300 import surrogate
+
+    types, lad, _ = surrogate.make_sequences(2, 1024, 17)
+    cfg = so.config()
+    with surrogate.Surrogate("", seed=9) as net:
+        p = net.params()
+        lay = so.layout(cfg)
+        off = sum(int(np.prod(s)) for n, s in lay[:-2])
+        p[off:off + 64] = np.random.default_rng(2).standard_normal(64) * 0.5
+        net.set_params(p)
+        got = net.predict(types, lad)
+        assert net.error_flags() == 0
+    ref = so.predict(p.astype(np.float64), cfg, types, lad)
+    ly_g, ly_r = np.log(got), np.log(ref)
+    assert np.abs(ly_g - ly_r).max() <= 2e-2 * max(1.0, np.abs(ly_r).max())
+
+
+@pytest.mark.gpu
 def test_network_gradients_match_oracle(engine_lib):
     from oracle import surrogate_oracle as so
     from tfm_gb300 import surrogate
