@@ -111,3 +111,7 @@ def test_screen_resimulates_random_and_out_of_envelope(engine_lib):
     assert len(set(fb.tolist()) - set(np.nonzero(out)[0])) <= 6
     err = rep["ps_error_random_sample"]
     assert np.isfinite([err["mean"], err["median"], err["p90"]]).all()
+    # the per-bin map error of the random sample, overall and by separation octave
+    me = rep["map_log10_error_random_sample"]
+    assert np.isfinite([me["mean"], me["median"], me["p90"]]).all() and me["mean"] >= 0
+    assert len(me["by_separation_octave"]) == int(np.log2(M // 2))

@@ -431,6 +431,20 @@ def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
     pb_sim = ps_log_bins(sim_maps)
     err = (np.abs(pb_pred[fb] - pb_sim) / np.maximum(pb_sim, 1e-12)).mean(axis=1)
     in_rand = np.isin(fb, rand)
+    # the re-simulated sequences' full maps, predicted again, against the
+    # simulation bin by bin: per map the mean |log10| difference, and over the
+    # random sample the mean difference of each separation octave's bins
+    pred_maps = np.concatenate([net.predict(types[fb[a:a + chunk]], lad[fb[a:a + chunk]])
+                                for a in range(0, len(fb), chunk)])
+    merr = map_log_error(pred_maps, sim_maps)
+    d = np.abs(np.log10(pred_maps[in_rand].astype(np.float64) + 1e-3)
+               - np.log10(np.asarray(sim_maps)[in_rand].astype(np.float64) + 1e-3)).mean(axis=0)
+    sep = np.abs(np.arange(bins)[:, None] - np.arange(bins)[None, :])
+    by_octave, a = [], 1
+    while a < bins // 2:
+        b = min(2 * a, bins // 2)
+        by_octave.append(float(d[(sep >= a) & (sep < b)].mean()))
+        a = b
     rep = {
         "sequences": int(n),
         "predict_s": t_pred,
@@ -442,7 +456,12 @@ def screen(net, types, lad, env, fallback_fraction, seed, sim, chunk=4096):
         "simulate_s": t_sim,
         "ps_error_random_sample": {"mean": float(err[in_rand].mean()), "median": float(np.median(err[in_rand])),
                                    "p90": float(np.percentile(err[in_rand], 90))},
+        "map_log10_error_random_sample": {
+            "mean": float(merr[in_rand].mean()), "median": float(np.median(merr[in_rand])),
+            "p90": float(np.percentile(merr[in_rand], 90)),
+            "by_separation_octave": by_octave},
     }
     if (~in_rand).any():
         rep["ps_error_out_of_envelope"] = float(err[~in_rand].mean())
+        rep["map_log10_error_out_of_envelope"] = float(merr[~in_rand].mean())
     return rep, fb
