@@ -47,6 +47,11 @@ PAIR_BYTES = 32.0  # pair kernel: read the cell-ordered float4, write the float4
 # dram__bytes_write.sum) from an ncu capture of the typed pair kernel on this
 # workload; a constant of that capture, not measured in the timed run
 PAIR_TRAFFIC_PER_BEAD = 58.9
+# warp instructions per bead of one pair launch (smsp__inst_executed.sum /
+# beads) from the same capture: the kernel is bound by instruction issue, so
+# its issue rate against 4 warp instructions per SM cycle is its roofline
+PAIR_WARP_INSTR_PER_BEAD = 108.8
+GB300_SMS = 152
 METRIC = "BD bead-steps/s (batched 512-replica ensemble, 1 GB300)"
 
 
@@ -411,6 +416,8 @@ def engine_arm(args, ws, rank, local):
                                                truth_reps=32, screen_n=100000)
 
     if rank == 0:
+        # the median SM clock of the timed region (else the GB300's maximum)
+        sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
         line = {
             "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -438,6 +445,15 @@ def engine_arm(args, ws, rank, local):
                                            "(a constant, not measured in this run)",
                          "bytes_per_bead": PAIR_BYTES,
                          "pair_ms": kt["pair"]},
+            "issue_roofline": None if args.replicas != 512 else {
+                "kernel": "pair", "unit": "warp instructions/s",
+                "achieved": total * PAIR_WARP_INSTR_PER_BEAD / pair_s,
+                "peak": GB300_SMS * 4 * sm_mhz * 1e6,
+                "frac": total * PAIR_WARP_INSTR_PER_BEAD / pair_s / (GB300_SMS * 4 * sm_mhz * 1e6),
+                "sm_mhz": sm_mhz,
+                "warp_instructions_per_bead": PAIR_WARP_INSTR_PER_BEAD,
+                "source": "instruction count from an ncu capture of this kernel on this "
+                          "workload (a constant); time and SM clock from this run"},
             "step_roofline": {"bytes_per_bead_step": B_ALG,
                               "achieved_gbs": value * B_ALG / 1e9,
                               "frac": value * B_ALG / 1e9 / hbm},
