@@ -497,6 +497,24 @@ def ccp_profile_sweep(sizes, steps=2000):
     return out
 
 
+def l2_copy_gbs(mb=32, reps=50):
+    """Copy bandwidth of a buffer pair that stays in the 129 MB L2 (read + write
+    bytes over CUDA-event time): the roofline of the L2-resident systems."""
+    import torch
+
+    a = torch.ones(mb * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    torch.cuda.synchronize()
+    return 2.0 * a.numel() * 4 * reps / (e0.elapsed_time(e1) / 1000.0) / 1e9
+
+
 def measure_extras(args, sizes, b):
     """Plain engine replica by replica, the large single system, the CPU baseline."""
     import torch
@@ -558,6 +576,14 @@ def measure_extras(args, sizes, b):
         "value": 2048 * HEUN_PER_STEP * 20 / (e0.elapsed_time(e1) / 1000.0),
         "unit": "bead-steps/s", "config": "c0: one chain of 2048 beads, contact map 2048^2"}
     c0.close()
+    # the single systems' state (<= ~15 MB) stays in L2: their step roofline
+    # is the L2 copy bandwidth, not HBM
+    l2 = l2_copy_gbs()
+    out["l2_copy_gbs"] = {"value": l2, "buffer": "2 x 32 MB, torch copy, CUDA events"}
+    for key in ("single_system_131072", "single_system_2048"):
+        v = out[key]["value"]
+        out[key]["l2_roofline"] = {"bytes_per_bead_step": B_ALG, "achieved_gbs": v * B_ALG / 1e9,
+                                   "peak_gbs": l2, "frac": v * B_ALG / 1e9 / l2}
     out["ccp_profile"] = ccp_profile_sweep([1024, 2048, 8192, 32768])
     # CPU baseline: the FP32 oracle on the first replicas' initial conditions
     pre = []
