@@ -159,7 +159,7 @@ int ccpgpu_kernel_times(ccpgpu_sim *h, int32_t reps, double *out, size_t n);
  * 0.75, 0.625, 0.55 and 0.5 times the largest cutoff (the last four with the
  * 5x5x5 stencil), keeps the fastest per class, keeps the faster kernel, then
  * picks the per-bead tile size (64, 128, 256) and the lanes per bead (1, 2,
- * 4; tile x lanes <= 512). Requires pair_kernel 2 or 4. Each
+ * 4, 8; tile x lanes <= 512). Requires pair_kernel 2 or 4. Each
  * candidate runs reps steps; positions, time and the noise counter are
  * restored afterwards. report receives a NUL-terminated JSON summary (size in
  * *len; CCPGPU_ERR_IO when cap is too small, after tuning). */

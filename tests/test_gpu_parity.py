@@ -130,12 +130,13 @@ def test_pair_kernels_agree(ccp_sim, base_sim, orc, kernel, half_cells):
         assert _force_ok(fo, f64, sa) <= 1e-2
 
 
-@pytest.mark.parametrize("kernel,lanes", [(2, 1), (2, 2), (2, 4), (4, 1), (4, 2), (4, 4)])
+@pytest.mark.parametrize("kernel,lanes", [(2, 1), (2, 2), (2, 4), (2, 8), (4, 1), (4, 2), (4, 4),
+                                          (4, 8)])
 def test_pair_lanes_agree(ccp_sim, base_sim, orc, kernel, lanes):
-    """The half-shell kernels (one grid, 2; typed layout, 4) with 1, 2 or 4
-    lanes per bead (rows dealt to the lanes, partial forces combined by
-    shuffles; small batches default to 4) meet the force bound, on cells of
-    half the cutoff."""
+    """The half-shell kernels (one grid, 2; typed layout, 4) with 1, 2, 4 or
+    8 lanes per bead (rows dealt to the lanes, partial forces combined by
+    shuffles; batches below 16384 beads default to 8) meet the force bound,
+    on cells of half the cutoff."""
     from tfm_gb300.ccpgpu import ChrSim
 
     sim, R = ccp_sim
@@ -416,7 +417,7 @@ def test_autotune_keeps_state_and_forces(engine_lib, orc):
     rep = b.autotune(reps=3)
     assert len(rep["classes"]) == 3 and rep["tile"] in (64, 128, 256)
     assert rep["pair_kernel"] in (2, 4) and len(rep["kernels_tried"]) == 2
-    assert rep["lanes"] in (1, 2, 4) and rep["tile"] * rep["lanes"] <= 512
+    assert rep["lanes"] in (1, 2, 4, 8) and rep["tile"] * rep["lanes"] <= 512
     assert np.array_equal(b.positions(), x0) and b.info().step == step0
     f = b.forces()
     pt, lbs = b.types(), b.lbs()

@@ -224,7 +224,8 @@ Params parse_params(const std::string &text) {
   p.pair_kernel = pm.get<int>("pair_kernel", p.preset == PRESET_BASELINE ? 4 : 2);
   if (!(p.pair_kernel >= 0 && p.pair_kernel <= 4)) fail("pair_kernel out of range");
   p.pair_lanes = pm.get<int>("pair_lanes", 0);  // 0: by the batch's bead count
-  if (!(p.pair_lanes == 0 || p.pair_lanes == 1 || p.pair_lanes == 2 || p.pair_lanes == 4))
+  if (!(p.pair_lanes == 0 || p.pair_lanes == 1 || p.pair_lanes == 2 || p.pair_lanes == 4 ||
+        p.pair_lanes == 8))
     fail("pair_lanes out of range");
   p.persistent = pm.get<int>("persistent", 0);
   if (!(p.persistent == 0 || p.persistent == 1)) fail("persistent out of range");
