@@ -80,3 +80,18 @@ def test_null_arguments_are_rejected(engine_lib):
 
     assert engine_lib.ccpgpu_create(None, 0, None) == ccpgpu.ERR_ARG
     assert engine_lib.ccpgpu_info_get(None, None) == ccpgpu.ERR_ARG
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_pair_lanes_values_parse(engine_lib, lanes):
+    """Every documented lanes-per-bead value passes the parameter checks (on a
+    machine without a GPU the call then fails at the device, not at them)."""
+    from tfm_gb300 import ccpgpu
+
+    h = C.c_void_p()
+    text = "force_field baseline\nnumber_of_particles 1000\npair_lanes %d\n" % lanes
+    rc = engine_lib.ccpgpu_create(text.encode(), 0, C.byref(h))
+    if rc == ccpgpu.OK:
+        engine_lib.ccpgpu_destroy(h)
+    else:
+        assert rc != ccpgpu.ERR_PARAM, engine_lib.ccpgpu_last_error().decode()
